@@ -1,0 +1,195 @@
+/*
+ * ngia.h — C ABI of the GB300 greedy sequence-clustering library (libngia.so).
+ *
+ * The reference program (nGIA, CUDA/signalNode) exposes its hot path as six
+ * in-process C++ calls declared in CUDA/signalNode/src/func.h:72-77
+ * (init, readIndex, readData, clustering, saveResult, finish) over the
+ * structs Option/Index/Data/Bench (func.h:14-70).  This header replaces
+ * that boundary with plain C entry points: every call returns an int status
+ * (0 = ok, negative = error; text via ngia_last_error), buffers are plain
+ * pointers plus sizes, and no CUDA or C++ type appears in a signature.
+ *
+ * Data model (identical to the makeDB database, makeDB/src/makeDB.cpp:1-16):
+ *   sequences are numbered in "sorted order" (raw length descending, ties
+ *   in FASTA order); record i is a run of uint32 words
+ *     DNA:     [len, net, cntA, cntC, cntG, cntT, {plane0, plane1} x ceil(len/32)]
+ *     protein: [len, net, cnt[28],               {plane0..plane4} x ceil(len/32)]
+ *   and records are contiguous in sorted order.
+ */
+#ifndef NGIA_H
+#define NGIA_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define NGIA_OK             0
+#define NGIA_E_ARG         -1   /* bad argument / null pointer               */
+#define NGIA_E_IO          -2   /* file missing, truncated or unreadable     */
+#define NGIA_E_FORMAT      -3   /* data.bin inconsistent (type word, sizes)  */
+#define NGIA_E_NOMEM       -4   /* host or device allocation failed          */
+#define NGIA_E_CUDA        -5   /* CUDA runtime error                        */
+#define NGIA_E_DEVICE      -6   /* device-side status (bounded wait expired) */
+#define NGIA_E_STATE       -7   /* call out of order                         */
+#define NGIA_E_LIMIT       -8   /* size beyond a documented maximum          */
+
+/* Copies the calling thread's last error message (NUL-terminated) into buf.
+ * Returns the status code of that error (0 if none). */
+int ngia_last_error(char *buf, size_t len);
+
+/* Library version string, e.g. "ngia-gb300 1.0". */
+const char *ngia_version(void);
+
+/* Frees any buffer this library returned through an out-pointer. */
+void ngia_free(void *p);
+
+/* ---- clustering parameters --------------------------------------------- */
+typedef struct ngia_params {
+    float   similarity;   /* -s : 0.1 .. 1.0                                  */
+    int32_t word_length;  /* -w : DNA 4..8, protein 2..3                      */
+    int32_t precise;      /* -p : 1 = skip the short-word filter              */
+} ngia_params;
+
+/* Applies the reference's parameter clamps in place for a database of the
+ * given type (0 DNA, 1 protein).  Replaces the clamp block of readIndex,
+ * CUDA/signalNode/src/func.cu:57-75. */
+int ngia_params_clamp(int32_t type, ngia_params *p);
+
+/* ---- database (host side) ---------------------------------------------- */
+typedef struct ngia_db_view {
+    int32_t         n;         /* number of sequences                          */
+    int32_t         type;      /* 0 DNA, 1 protein                             */
+    int32_t         longest;   /* raw length of sequence 0                     */
+    int32_t         shortest;  /* raw length of sequence n-1                   */
+    const uint32_t *words;     /* all records, contiguous, sorted order        */
+    int64_t         n_words;
+    const int64_t  *rec_off;   /* word offset of each record inside words      */
+} ngia_db_view;
+
+typedef struct ngia_db_host {
+    ngia_db_view view;
+    int32_t *name_len;         /* header length incl. '>' (data.bin index)     */
+    int32_t *read_len;         /* raw sequence length                          */
+    int64_t *fasta_off;        /* byte offset of the record's '>' in data.fasta */
+    int64_t *pack_off;         /* byte offset of the record in data.bin        */
+} ngia_db_host;
+
+/* Reads <dir>/data.bin: header, index and all records into host memory.
+ * Replaces readIndex + readData, CUDA/signalNode/src/func.cu:42-154. */
+int ngia_db_load(const char *dir, ngia_db_host **out);
+
+/* Packs raw sequences (given in FASTA order) into an in-memory database laid
+ * out exactly as makeDB would write it: records longer than 65,536 are
+ * dropped, the rest stable-sorted by raw length descending and bit-plane
+ * packed (makeDB/src/makeDB.cpp:62-106, 108-252).  name_len may be NULL
+ * (then every header is taken as 1 byte long and fasta_off is 0). */
+int ngia_db_pack(int32_t type, const char *seq, const int64_t *seq_off,
+                 int64_t n, const int32_t *name_len, ngia_db_host **out);
+
+/* Builds <outdir>/data.bin and the <outdir>/data.fasta symlink from a FASTA
+ * file; the drop-in for the makeDB tool (makeDB/src/makeDB.cpp:254-334). */
+int ngia_makedb(const char *fasta_path, const char *outdir, int32_t type);
+
+/* Writes <outdir>/cluster.txt and <outdir>/represent.fasta from a cluster
+ * assignment (cluster[i] = representative of sequence i, sorted order),
+ * reading names and residues from <dbdir>/data.fasta.  Replaces saveResult,
+ * CUDA/signalNode/src/func.cu:680-764.  *n_clusters receives the count the
+ * reference prints as "Cluster:\t<n>". */
+int ngia_save_result(const char *dbdir, const char *outdir,
+                     const ngia_db_host *db, const int32_t *cluster,
+                     int32_t *n_clusters);
+
+void ngia_db_free(ngia_db_host *db);
+
+/* ---- synthetic inputs (seeded; same bytes on x86-64 and aarch64) -------- */
+typedef struct ngia_synth_params {
+    int32_t  type;         /* 0 DNA (ACGT), 1 protein (20 residues)            */
+    int32_t  len_dist;     /* 0 normal(a,b)  1 lognormal(median a, sigma b)    */
+                           /* 2 loguniform[a,b]                                */
+    int64_t  n_seqs;
+    int32_t  n_ancestors;
+    int32_t  len_min, len_max;  /* clip range of ancestor lengths             */
+    double   len_a, len_b;
+    double   subst_max;    /* per-sequence substitution rate ~ U[0,subst_max] */
+    double   indel_frac;   /* indel event rate = indel_frac * substitution    */
+    int32_t  indel_max;    /* indel length ~ U{1..indel_max}                  */
+    double   novel_frac;   /* share of sequences taken from extra ancestors   */
+    uint64_t seed;
+} ngia_synth_params;
+
+/* Generates sequences in FASTA order: *seq holds all residues back to back,
+ * (*seq_off)[i] .. (*seq_off)[i+1] delimits sequence i (n+1 offsets).
+ * Free both with ngia_free. */
+int ngia_synth_generate(const ngia_synth_params *p, char **seq,
+                        int64_t **seq_off, int64_t *n);
+
+/* Writes sequences as FASTA (headers ">s<i>", lines of `width` residues). */
+int ngia_write_fasta(const char *path, const char *seq, const int64_t *seq_off,
+                     int64_t n, int32_t width);
+
+/* ---- device clustering -------------------------------------------------- */
+typedef struct ngia_ctx ngia_ctx;
+
+/* Driver forms of the greedy loop. */
+#define NGIA_MODE_PLAIN  0  /* host loop: one launch sequence per representative */
+#define NGIA_MODE_GRAPH  1  /* device-side driver in a captured CUDA graph
+                               (conditional while node), no host round trip  */
+
+typedef struct ngia_stats {
+    int64_t iterations;    /* representatives taken (= clusters)             */
+    int64_t candidates;    /* (representative, candidate) visits             */
+    int64_t base_pass;     /* visits passing the composition filter          */
+    int64_t align_pairs;   /* pairs entering the alignment stage             */
+    int64_t members;       /* pairs accepted (incl. each representative)     */
+    int64_t band_cells;    /* reference band cells of the alignment pairs    */
+    int64_t filter_bytes;  /* algorithmic filter bytes (headers + planes)    */
+    int64_t word_checks;   /* pairs the short-word filter was evaluated on   */
+} ngia_stats;
+
+/* Copies the database to the device (one host-to-device transfer) and
+ * builds the per-sequence header arrays.  Replaces the device half of
+ * readData, CUDA/signalNode/src/func.cu:104-154.  The caller keeps
+ * ownership of the host buffers. */
+int ngia_open(const ngia_db_view *db, ngia_ctx **out);
+
+/* Full greedy clustering.  Replaces clustering(),
+ * CUDA/signalNode/src/func.cu:607-677.  cluster_out[n] receives the
+ * representative (sorted index) of every sequence; identity_out[n] (may be
+ * NULL) the banded-LCS score each member reached against its representative
+ * (-1 for a representative that failed its own tests).  stats may be NULL. */
+int ngia_cluster(ngia_ctx *ctx, const ngia_params *p, int32_t mode,
+                 int32_t *cluster_out, int32_t *identity_out,
+                 ngia_stats *stats);
+
+/* Stepwise form of ngia_cluster for benchmarking and checkpointing:
+ * begin resets the state; step runs up to max_iters representatives
+ * (all remaining if max_iters <= 0) and reports *done; end copies results. */
+int ngia_cluster_begin(ngia_ctx *ctx, const ngia_params *p, int32_t mode);
+int ngia_cluster_step(ngia_ctx *ctx, int64_t max_iters, int32_t *done);
+int ngia_cluster_end(ngia_ctx *ctx, int32_t *cluster_out,
+                     int32_t *identity_out, ngia_stats *stats);
+
+/* Per-pair stage values for (rep, cands[k]) pairs, for unit-level parity:
+ * out[4k+0] = composition sum, out[4k+1] = short-word count (-1 when the
+ * reference skips it because a net length is < 16), out[4k+2] = banded-LCS
+ * score, out[4k+3] = block band.  Mirrors the per-job bodies of the six
+ * reference kernels, CUDA/signalNode/src/func.cu:323-604. */
+int ngia_pair_scores(ngia_ctx *ctx, const ngia_params *p, int32_t rep,
+                     const int32_t *cands, int32_t n, int32_t *out);
+
+/* Number of CUDA devices visible to the process (0 when there is none). */
+int ngia_device_count(int32_t *count);
+
+/* CUDA stream the context launches on (as an opaque handle, for timing). */
+void *ngia_stream(ngia_ctx *ctx);
+
+int ngia_close(ngia_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NGIA_H */

@@ -1,0 +1,749 @@
+// align.cu — banded bit-parallel LCS identity kernels (the reference's
+// kernel_dynamicGen/Pro, CUDA/signalNode/src/func.cu:450-604).
+//
+// The reference computes, per (representative, query) pair, a block-banded
+// form of the Allison–Dix / Hyyrö bit-vector LCS: the representative's net
+// residues are the rows (32 per word, line[j]), the query's net residues the
+// columns, processed in 32-column blocks i.  For query block i only rep
+// blocks j in [max(i-B,0), min(i+B,nb1-1)] are updated, with
+// B = (ceil(fma(-L2,s,L1)) + 31)/32; the carry into the lowest band block is
+// 0 and the carry out of the highest is dropped; blocks outside the band keep
+// their state.  The score is the number of zero bits of line[] over the net
+// length, accepted when >= ceil(L2*s).
+//
+// Two kernels reproduce that exactly:
+//
+// k_align_win<P,WC>  one thread per pair.  The band window (at most WC rep
+//   blocks) lives in registers: row[m] and the rep's planes pl[p][m] for
+//   slot m = rep block js+m.  For each query residue the whole window is
+//   updated as one multi-word addition whose carries ride the hardware carry
+//   flag (add.cc/addc.cc), i.e. four integer instructions per 32 cells for DNA
+//   (two LOP3 for the match mask, one IADD3.X, one LOP3 for the row).  When
+//   the band slides, the departing block's zero count is banked and the
+//   registers shift down one slot; an entering block starts all-ones.  Lanes
+//   claim pairs from the class queue independently (warp-aggregated atomics).
+//
+// k_align_generic<P>  any band width: one thread per pair in the reference's
+//   (i, j, k) order with line[] in global scratch and the 32 column carries
+//   packed into one word.
+//
+// Both stop a pair early once it provably cannot reach the cutoff: each query
+// residue raises the counted zeros by at most one (the bit-vector update only
+// moves a zero downwards within a run of ones, or adds one at the top of the
+// updated segment), so zeros_now + residues_left < cutoff is a rejection.
+// Accepted pairs are always computed to the end (their score is reported).
+#include <climits>
+
+#include "ctx.h"
+
+namespace ngia {
+
+constexpr int kRepPlanesOff = 32;  // planes offset inside rb.rep_rec (filter.cu)
+constexpr int kAlignThreads = 128;  // threads per CTA of every alignment kernel
+
+// Resident CTAs per SM requested from the register allocator for the
+// register-window kernel of P planes and WC slots.
+__host__ __device__ constexpr int win_min_blocks(int P, int WC) {
+  return P == 2 ? (WC <= 8 ? 6 : WC <= 16 ? 4 : WC <= 24 ? 3 : 2) : (WC <= 8 ? 4 : 2);
+}
+
+// ---- multi-word addition on the carry flag -------------------------------------
+// t[0..7] = r[0..7] + x[0..7] (+ carry in), least significant word first.
+template <bool FIRST, bool LAST>
+struct Add8;
+
+template <>
+struct Add8<true, true> {
+  static __device__ __forceinline__ void run(const uint32_t *r, const uint32_t *x, uint32_t *t, uint32_t &) {
+    asm("add.cc.u32 %0, %8, %16;\n\t"
+        "addc.cc.u32 %1, %9, %17;\n\t"
+        "addc.cc.u32 %2, %10, %18;\n\t"
+        "addc.cc.u32 %3, %11, %19;\n\t"
+        "addc.cc.u32 %4, %12, %20;\n\t"
+        "addc.cc.u32 %5, %13, %21;\n\t"
+        "addc.cc.u32 %6, %14, %22;\n\t"
+        "addc.u32 %7, %15, %23;"
+        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7])
+        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(x[0]),
+          "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]));
+  }
+};
+template <>
+struct Add8<true, false> {
+  static __device__ __forceinline__ void run(const uint32_t *r, const uint32_t *x, uint32_t *t, uint32_t &c) {
+    asm("add.cc.u32 %0, %9, %17;\n\t"
+        "addc.cc.u32 %1, %10, %18;\n\t"
+        "addc.cc.u32 %2, %11, %19;\n\t"
+        "addc.cc.u32 %3, %12, %20;\n\t"
+        "addc.cc.u32 %4, %13, %21;\n\t"
+        "addc.cc.u32 %5, %14, %22;\n\t"
+        "addc.cc.u32 %6, %15, %23;\n\t"
+        "addc.cc.u32 %7, %16, %24;\n\t"
+        "addc.u32 %8, 0, 0;"
+        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7]),
+          "=r"(c)
+        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(x[0]),
+          "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]));
+  }
+};
+template <>
+struct Add8<false, true> {
+  static __device__ __forceinline__ void run(const uint32_t *r, const uint32_t *x, uint32_t *t, uint32_t &c) {
+    asm("{\n\t.reg .u32 d;\n\t"
+        "add.cc.u32 d, %24, 0xFFFFFFFF;\n\t"
+        "addc.cc.u32 %0, %8, %16;\n\t"
+        "addc.cc.u32 %1, %9, %17;\n\t"
+        "addc.cc.u32 %2, %10, %18;\n\t"
+        "addc.cc.u32 %3, %11, %19;\n\t"
+        "addc.cc.u32 %4, %12, %20;\n\t"
+        "addc.cc.u32 %5, %13, %21;\n\t"
+        "addc.cc.u32 %6, %14, %22;\n\t"
+        "addc.u32 %7, %15, %23;\n\t}"
+        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7])
+        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(x[0]),
+          "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]), "r"(c));
+  }
+};
+template <>
+struct Add8<false, false> {
+  static __device__ __forceinline__ void run(const uint32_t *r, const uint32_t *x, uint32_t *t, uint32_t &c) {
+    asm("{\n\t.reg .u32 d;\n\t"
+        "add.cc.u32 d, %25, 0xFFFFFFFF;\n\t"
+        "addc.cc.u32 %0, %9, %17;\n\t"
+        "addc.cc.u32 %1, %10, %18;\n\t"
+        "addc.cc.u32 %2, %11, %19;\n\t"
+        "addc.cc.u32 %3, %12, %20;\n\t"
+        "addc.cc.u32 %4, %13, %21;\n\t"
+        "addc.cc.u32 %5, %14, %22;\n\t"
+        "addc.cc.u32 %6, %15, %23;\n\t"
+        "addc.cc.u32 %7, %16, %24;\n\t"
+        "addc.u32 %8, 0, 0;\n\t}"
+        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7]),
+          "=r"(c)
+        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(x[0]),
+          "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]), "r"(c));
+  }
+};
+
+// One query residue over the whole register window: x = row & match,
+// row = (row + x (+ carries)) | (row & ~match).
+template <int P, int WC>
+__device__ __forceinline__ void dp_column(uint32_t (&row)[WC], const uint32_t (&pl)[P][WC], const uint32_t (&mk)[P]) {
+  // 8 slots at a time end to end, so only 16 temporaries are live beside the
+  // window; the carry between chunks travels in a register.
+  uint32_t carry = 0;
+#pragma unroll
+  for (int ch = 0; ch < WC / 8; ch++) {
+    uint32_t x[8], t[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int m = 8 * ch + q;
+      uint32_t a = row[m];
+#pragma unroll
+      for (int p = 0; p < P; p++) a &= ~(pl[p][m] ^ mk[p]);
+      x[q] = a;
+    }
+    const uint32_t *rr = row + 8 * ch;
+    if (WC == 8)
+      Add8<true, true>::run(rr, x, t, carry);
+    else if (ch == 0)
+      Add8<true, false>::run(rr, x, t, carry);
+    else if (ch == WC / 8 - 1)
+      Add8<false, true>::run(rr, x, t, carry);
+    else
+      Add8<false, false>::run(rr, x, t, carry);
+#pragma unroll
+    for (int q = 0; q < 8; q++) row[8 * ch + q] = t[q] | (row[8 * ch + q] ^ x[q]);
+  }
+}
+
+struct AlignHdr {
+  int qn, L1, net1, nb1, word_after, rep;
+};
+
+// Reads the iteration header and stages the representative's planes (and,
+// when the short-word test follows the alignment, its k-mer bitset) into
+// shared memory with bulk copies.  Returns false when there is no work.
+template <int P>
+__device__ __forceinline__ bool align_setup(const DevDB &db, const RunBufs &rb, const RunParams &prm, int cls,
+                                            int score_mode, uint32_t *smem, uint64_t *bar, AlignHdr &h) {
+  __shared__ int s_hdr[6];
+  RunState *st = rb.st;
+  if (threadIdx.x == 0) {
+    const bool skip = !score_mode && (st->done || st->iter >= st->iter_limit || st->err);
+    s_hdr[0] = skip ? 0 : (int)st->qcount[cls];
+    s_hdr[1] = st->rep_len;
+    s_hdr[2] = st->rep_net;
+    s_hdr[3] = st->rep_nb;
+    s_hdr[4] = !score_mode && st->word_active && !st->word_first;
+    s_hdr[5] = st->rep;
+  }
+  __syncthreads();
+  h.qn = s_hdr[0];
+  if (h.qn == 0) return false;
+  h.L1 = s_hdr[1];
+  h.net1 = s_hdr[2];
+  h.nb1 = s_hdr[3];
+  h.word_after = s_hdr[4];
+  h.rep = s_hdr[5];
+  const uint32_t plane_words = (uint32_t)((h.nb1 * P + 3) & ~3);
+  const uint32_t list_words = h.word_after ? (uint32_t)max(4, (int)((1u << (prm.w * (P == 2 ? 2 : 5))) / 32u)) : 0u;
+  if (threadIdx.x == 0) {
+    mbar_init(bar, 1);
+    const uint32_t bytes = 4u * (plane_words + list_words);
+    if (bytes) {
+      mbar_expect_tx(bar, bytes);
+      if (plane_words) bulk_g2s(smem, rb.rep_rec + kRepPlanesOff, 4u * plane_words, bar);
+      if (list_words) bulk_g2s(smem + plane_words, rb.rep_list, 4u * list_words, bar);
+    } else {
+      asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+    }
+  }
+  __syncthreads();
+  bool ok = mbar_wait_bounded(bar, 0, 1u << 20);
+  if (!ok) {
+    set_error(st, NGIA_ERR_MBAR_TIMEOUT, 10 + cls);
+    mbar_wait_bounded(bar, 0, 1u << 20);
+  }
+  return __syncthreads_and(ok);
+}
+
+// Claims the next queue entry for every idle lane with one atomic per warp.
+// state: -1 idle, -2 queue exhausted, >= 0 the claimed entry.
+__device__ __forceinline__ void claim(RunState *st, int cls, int qn, int lane, int &state) {
+  const bool need = state == -1;
+  const unsigned nm = __ballot_sync(kFullMask, need);
+  if (!nm) return;
+  const int leader = __ffs(nm) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(&st->qhead[cls], (uint32_t)__popc(nm));
+  base = __shfl_sync(kFullMask, base, leader);
+  if (need) {
+    const uint32_t idx = base + (uint32_t)__popc(nm & ((1u << lane) - 1u));
+    state = idx < (uint32_t)qn ? (int)idx : -2;
+  }
+}
+
+// Outcome of one pair: membership (or the pair score in score mode).
+template <int P>
+__device__ __forceinline__ void finish_pair(const DevDB &db, const RunBufs &rb, const RunParams &prm,
+                                            const AlignHdr &h, int score_mode, int entry, int cand, int sum,
+                                            int cutoff, int L2, int net2, const uint32_t *qpl,
+                                            const uint32_t *s_list, unsigned long long &members) {
+  if (score_mode) {
+    rb.score_out[4 * entry + 2] = sum;
+    return;
+  }
+  bool pass = !(sum < cutoff);
+  if (pass && h.word_after) {
+    // short-word test of func.cu:376-396, evaluated only for aligned members
+    int ws = 0;
+    {
+      constexpr int bits = P == 2 ? 2 : 5;
+      const uint32_t mask = (1u << (prm.w * bits)) - 1u;
+      uint32_t word = 0;
+      for (int i = 0; i < net2; i += 32) {
+        uint32_t pl[P];
+#pragma unroll
+        for (int p = 0; p < P; p++) pl[p] = qpl[(i >> 5) * P + p];
+        const int lim = min(32, net2 - i);
+        for (int j = 0; j < lim; j++) {
+          uint32_t c = 0;
+#pragma unroll
+          for (int p = 0; p < P; p++) c |= ((pl[p] >> j) & 1u) << p;
+          word = ((word << bits) | c) & mask;
+          if (i + j >= prm.w - 1) ws += (s_list[word >> 5] >> (word & 31)) & 1u;
+        }
+      }
+    }
+    pass = !(ws < word_min(L2, prm.w, prm.s));
+  }
+  if (pass) {
+    rb.cluster[cand] = h.rep;
+    rb.ident[cand] = sum;
+    atomicAnd(&rb.alive[cand >> 5], ~(1u << (cand & 31)));
+    members++;
+  }
+}
+
+__device__ __forceinline__ void flush_align_stats(RunState *st, unsigned long long pairs,
+                                                  unsigned long long members, unsigned long long cells) {
+  for (int o = 16; o; o >>= 1) {
+    pairs += __shfl_down_sync(kFullMask, pairs, o);
+    members += __shfl_down_sync(kFullMask, members, o);
+    cells += __shfl_down_sync(kFullMask, cells, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    if (pairs) atomicAdd(&st->st_align_pairs, pairs);
+    if (members) atomicAdd(&st->st_members, members);
+    if (cells) atomicAdd(&st->st_band_cells, cells);
+  }
+}
+
+template <int P, int WC>
+__global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_win(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ uint64_t bar;
+  AlignHdr h;
+  if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
+  const uint32_t *s_pl = smem;
+  const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
+  RunState *st = rb.st;
+  const int lane = threadIdx.x & 31;
+  const float s = prm.s;
+  const int nb1 = h.nb1;
+  const uint32_t vlast = (h.net1 & 31) ? ((1u << (h.net1 & 31)) - 1u) : 0xFFFFFFFFu;
+
+  uint32_t row[WC], pl[P][WC], cur[P], nxt[P];
+  int state = -1, entry = 0, cand = 0;
+  int i = 0, nq = 0, B = 0, js = 0, je = -1, net2 = 0, L2 = 0, cutoff = 0, lastcols = 32, frozen = 0;
+  const uint32_t *qpl = nullptr;
+  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0;
+
+  for (;;) {
+    claim(st, cls, h.qn, lane, state);
+    if (__all_sync(kFullMask, state == -2)) break;
+    if (state < 0) continue;
+    // ---- start of a newly claimed pair -----------------------------------
+    if (qpl == nullptr) {
+      entry = rb.queue[cls][state];  // candidate, or pair slot in score mode
+      cand = score_mode ? rb.score_cands[entry] : entry;
+      L2 = __ldg(db.len + cand);
+      net2 = __ldg(db.net + cand);
+      nq = (net2 + 31) >> 5;
+      lastcols = (net2 & 31) ? (net2 & 31) : 32;
+      B = band_blocks(h.L1, L2, s);
+      cutoff = cutoff_of(L2, s);
+      qpl = db.words + __ldg(db.off + cand) + db.hw;
+      i = 0;
+      js = 0;
+      je = min(B, nb1 - 1);
+      frozen = 0;
+      if (!score_mode) {
+        n_pairs++;
+        n_cells += (unsigned long long)band_cells(B, nb1, net2);
+      }
+      if (B < 0 || je < 0 || nq == 0) {
+        finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, 0, cutoff, L2, net2, qpl, s_list, n_members);
+        qpl = nullptr;
+        state = -1;
+        continue;
+      }
+#pragma unroll
+      for (int m = 0; m < WC; m++) {
+        row[m] = 0xFFFFFFFFu;
+#pragma unroll
+        for (int p = 0; p < P; p++) pl[p][m] = (m <= je) ? s_pl[m * P + p] : 0u;
+      }
+#pragma unroll
+      for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
+    }
+    // ---- one 32-residue query block ---------------------------------------
+    const int cols = (i == nq - 1) ? lastcols : 32;
+    if (i + 1 < nq) {
+#pragma unroll
+      for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
+    }
+    uint32_t rv[P];
+#pragma unroll
+    for (int p = 0; p < P; p++) rv[p] = __brev(cur[p]);
+    int k = 0;
+    for (; k + 2 <= cols; k += 2) {
+      uint32_t mk[P];
+#pragma unroll
+      for (int p = 0; p < P; p++) {
+        mk[p] = (uint32_t)((int)rv[p] >> 31);
+        rv[p] <<= 1;
+      }
+      dp_column<P, WC>(row, pl, mk);
+#pragma unroll
+      for (int p = 0; p < P; p++) {
+        mk[p] = (uint32_t)((int)rv[p] >> 31);
+        rv[p] <<= 1;
+      }
+      dp_column<P, WC>(row, pl, mk);
+    }
+    if (k < cols) {
+      uint32_t mk[P];
+#pragma unroll
+      for (int p = 0; p < P; p++) mk[p] = (uint32_t)((int)rv[p] >> 31);
+      dp_column<P, WC>(row, pl, mk);
+    }
+    // ---- slide the band to query block i+1 --------------------------------
+    i++;
+    bool finished = i >= nq;
+    if (!finished) {
+      if (i - B > 0) {  // js advances: block js leaves the band for good
+        frozen += __popc(~row[0] & (js == nb1 - 1 ? vlast : 0xFFFFFFFFu));
+#pragma unroll
+        for (int m = 0; m < WC - 1; m++) {
+          row[m] = row[m + 1];
+#pragma unroll
+          for (int p = 0; p < P; p++) pl[p][m] = pl[p][m + 1];
+        }
+        js++;
+      }
+      if (i + B <= nb1 - 1) {  // je advances: block je enters all-ones
+        je++;
+        const int slot = je - js;
+        uint32_t v[P];
+#pragma unroll
+        for (int p = 0; p < P; p++) v[p] = s_pl[je * P + p];
+#pragma unroll
+        for (int m = 0; m < WC; m++)
+          if (m == slot) {
+            row[m] = 0xFFFFFFFFu;
+#pragma unroll
+            for (int p = 0; p < P; p++) pl[p][m] = v[p];
+          }
+      }
+      if (js > je) finished = true;  // band ran past the representative
+    }
+    const int n = je - js + 1;
+    if (finished) {
+      int sum = frozen;
+#pragma unroll
+      for (int m = 0; m < WC; m++)
+        if (m < n) sum += __popc(~row[m] & (js + m == nb1 - 1 ? vlast : 0xFFFFFFFFu));
+      finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, sum, cutoff, L2, net2, qpl, s_list, n_members);
+      qpl = nullptr;
+      state = -1;
+      continue;
+    }
+    if (!score_mode) {
+      int z = frozen;
+#pragma unroll
+      for (int m = 0; m < WC; m++) z += (m < n) ? __popc(~row[m]) : 0;
+      if (z + (net2 - 32 * i) < cutoff) {  // cannot reach the cutoff any more
+        qpl = nullptr;
+        state = -1;
+        continue;
+      }
+    }
+#pragma unroll
+    for (int p = 0; p < P; p++) cur[p] = nxt[p];
+  }
+  flush_align_stats(st, n_pairs, n_members, n_cells);
+}
+
+
+// One query residue over a TW-slot register tile whose carry enters from and
+// leaves to a register (the tiles of one window are chained through it).
+template <int P, int TW>
+__device__ __forceinline__ void dp_tile_column(uint32_t (&row)[TW], const uint32_t (&pl)[P][TW],
+                                               const uint32_t (&mk)[P], uint32_t &carry) {
+#pragma unroll
+  for (int ch = 0; ch < TW / 8; ch++) {
+    uint32_t x[8], t[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int m = 8 * ch + q;
+      uint32_t a = row[m];
+#pragma unroll
+      for (int p = 0; p < P; p++) a &= ~(pl[p][m] ^ mk[p]);
+      x[q] = a;
+    }
+    Add8<false, false>::run(row + 8 * ch, x, t, carry);
+#pragma unroll
+    for (int q = 0; q < 8; q++) row[8 * ch + q] = t[q] | (row[8 * ch + q] ^ x[q]);
+  }
+}
+
+// Tiled window: windows of up to kRingBlocks rep blocks.  Each lane keeps its
+// pair's band rows in a shared-memory ring indexed by absolute rep block
+// (ring[(j mod kRingBlocks) * threads + tid], so the 32 lanes of a warp hit 32
+// distinct banks whatever their j), and runs each query block tile by tile
+// over 16-slot register tiles in ascending rep-block order, all 32 residues
+// per tile, passing the 32 column carries between tiles in one word.  This is
+// the reference's (i, j, k) loop order at tile granularity.
+template <int P>
+__global__ void __launch_bounds__(kAlignThreads, P == 2 ? 3 : 2)
+    k_align_tiled(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode) {
+  constexpr int TW = 16;
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ uint64_t bar;
+  AlignHdr h;
+  if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
+  const uint32_t *s_pl = smem;
+  const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
+  uint32_t *ring = smem + (((db.max_nb * P + 3) & ~3) + kListWords) + threadIdx.x;
+  constexpr int RS = kAlignThreads;  // ring stride
+  RunState *st = rb.st;
+  const int lane = threadIdx.x & 31;
+  const float s = prm.s;
+  const int nb1 = h.nb1;
+  const uint32_t vlast = (h.net1 & 31) ? ((1u << (h.net1 & 31)) - 1u) : 0xFFFFFFFFu;
+
+  int state = -1, entry = 0, cand = 0;
+  int i = 0, nq = 0, B = 0, js = 0, je = -1, net2 = 0, L2 = 0, cutoff = 0, lastcols = 32, frozen = 0, zw = 0;
+  bool active = false;
+  const uint32_t *qpl = nullptr;
+  uint32_t cur[P], nxt[P];
+  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0;
+  for (;;) {
+    claim(st, cls, h.qn, lane, state);
+    if (__all_sync(kFullMask, state == -2)) break;
+    if (state < 0) continue;
+    if (!active) {
+      entry = rb.queue[cls][state];
+      cand = score_mode ? rb.score_cands[entry] : entry;
+      L2 = __ldg(db.len + cand);
+      net2 = __ldg(db.net + cand);
+      nq = (net2 + 31) >> 5;
+      lastcols = (net2 & 31) ? (net2 & 31) : 32;
+      B = band_blocks(h.L1, L2, s);
+      cutoff = cutoff_of(L2, s);
+      qpl = db.words + __ldg(db.off + cand) + db.hw;
+      i = 0;
+      js = 0;
+      je = min(B, nb1 - 1);
+      frozen = 0;
+      zw = 0;
+      if (!score_mode) {
+        n_pairs++;
+        n_cells += (unsigned long long)band_cells(B, nb1, net2);
+      }
+      if (B < 0 || je < 0 || nq == 0) {
+        finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, 0, cutoff, L2, net2, qpl, s_list, n_members);
+        state = -1;
+        continue;
+      }
+      for (int j = 0; j <= je; j++) ring[(j & (kRingBlocks - 1)) * RS] = 0xFFFFFFFFu;
+#pragma unroll
+      for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
+      active = true;
+    }
+    const int cols = (i == nq - 1) ? lastcols : 32;
+    if (i + 1 < nq) {
+#pragma unroll
+      for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
+    }
+    uint32_t cw = 0;  // column carries entering the current tile
+    for (int base = js; base <= je; base += TW) {
+      uint32_t row[TW], pl[P][TW];
+      int zold = 0;
+#pragma unroll
+      for (int m = 0; m < TW; m++) {
+        const int j = base + m;
+        const bool in = j <= je;
+        row[m] = in ? ring[(j & (kRingBlocks - 1)) * RS] : 0u;
+        zold += in ? __popc(~row[m]) : 0;
+#pragma unroll
+        for (int p = 0; p < P; p++) pl[p][m] = in ? s_pl[j * P + p] : 0u;
+      }
+      uint32_t rv[P];
+#pragma unroll
+      for (int p = 0; p < P; p++) rv[p] = __brev(cur[p]);
+      uint32_t cin = cw, cout = 0;
+      for (int k = 0; k < cols; k++) {
+        uint32_t mk[P];
+#pragma unroll
+        for (int p = 0; p < P; p++) {
+          mk[p] = (uint32_t)((int)rv[p] >> 31);
+          rv[p] <<= 1;
+        }
+        uint32_t carry = cin & 1u;
+        cin >>= 1;
+        dp_tile_column<P, TW>(row, pl, mk, carry);
+        cout |= carry << k;
+      }
+      int znew = 0;
+#pragma unroll
+      for (int m = 0; m < TW; m++) {
+        const int j = base + m;
+        if (j <= je) {
+          ring[(j & (kRingBlocks - 1)) * RS] = row[m];
+          znew += __popc(~row[m]);
+        }
+      }
+      zw += znew - zold;
+      cw = cout;
+    }
+    i++;
+    bool finished = i >= nq;
+    if (!finished) {
+      if (i - B > 0) {  // block js leaves the band
+        const uint32_t r0 = ring[(js & (kRingBlocks - 1)) * RS];
+        frozen += __popc(~r0 & (js == nb1 - 1 ? vlast : 0xFFFFFFFFu));
+        zw -= __popc(~r0);
+        js++;
+      }
+      if (i + B <= nb1 - 1) {  // block je enters all-ones
+        je++;
+        ring[(je & (kRingBlocks - 1)) * RS] = 0xFFFFFFFFu;
+      }
+      if (js > je) finished = true;
+    }
+    if (finished) {
+      int sum = frozen;
+      for (int j = js; j <= je; j++)
+        sum += __popc(~ring[(j & (kRingBlocks - 1)) * RS] & (j == nb1 - 1 ? vlast : 0xFFFFFFFFu));
+      finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, sum, cutoff, L2, net2, qpl, s_list, n_members);
+      active = false;
+      state = -1;
+      continue;
+    }
+    if (!score_mode && frozen + zw + (net2 - 32 * i) < cutoff) {
+      active = false;
+      state = -1;
+      continue;
+    }
+#pragma unroll
+    for (int p = 0; p < P; p++) cur[p] = nxt[p];
+  }
+  flush_align_stats(st, n_pairs, n_members, n_cells);
+}
+
+template <int P>
+__global__ void __launch_bounds__(kAlignThreads) k_align_generic(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ uint64_t bar;
+  AlignHdr h;
+  if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
+  const uint32_t *s_pl = smem;
+  const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
+  RunState *st = rb.st;
+  const int lane = threadIdx.x & 31;
+  const float s = prm.s;
+  const int nb1 = h.nb1;
+  const uint32_t vlast = (h.net1 & 31) ? ((1u << (h.net1 & 31)) - 1u) : 0xFFFFFFFFu;
+  const int64_t gl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t TL = (int64_t)gridDim.x * blockDim.x;
+  if ((int64_t)nb1 * TL > rb.scratch_words) {
+    if (threadIdx.x == 0) set_error(st, NGIA_ERR_SCRATCH, 20);
+    return;
+  }
+  uint32_t *line = rb.scratch + gl;  // line[j] at line[j * TL]
+
+  int state = -1, entry = 0, cand = 0, i = 0, nq = 0, B = 0, net2 = 0, L2 = 0, cutoff = 0, zc = 0;
+  bool busy = false;
+  const uint32_t *qpl = nullptr;
+  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0;
+  for (;;) {
+    claim(st, cls, h.qn, lane, state);
+    if (__all_sync(kFullMask, state == -2)) break;
+    if (state < 0) continue;
+    if (!busy) {
+      const int e = rb.queue[cls][state];
+      cand = score_mode ? rb.score_cands[e] : e;
+      entry = e;
+      L2 = db.len[cand];
+      net2 = db.net[cand];
+      nq = (net2 + 31) >> 5;
+      B = band_blocks(h.L1, L2, s);
+      cutoff = cutoff_of(L2, s);
+      qpl = db.words + db.off[cand] + db.hw;
+      if (!score_mode) {
+        n_pairs++;
+        n_cells += (unsigned long long)band_cells(B, nb1, net2);
+      }
+      for (int j = 0; j < nb1; j++) line[j * TL] = 0xFFFFFFFFu;
+      i = 0;
+      zc = 0;
+      busy = true;
+    }
+    if (i < nq) {
+      const int cols = ((i + 1) * 32 > net2) ? (net2 & 31) : 32;
+      uint32_t col[P];
+#pragma unroll
+      for (int p = 0; p < P; p++) col[p] = qpl[i * P + p];
+      const int jstart = max(i - B, 0), jend = min(i + B, nb1 - 1);
+      uint32_t cw = 0;
+      for (int j = jstart; j <= jend; j++) {
+        uint32_t R[P];
+#pragma unroll
+        for (int p = 0; p < P; p++) R[p] = s_pl[j * P + p];
+        const uint32_t old = line[j * TL];
+        uint32_t row = old, ncw = 0;
+        for (int k = 0; k < cols; k++) {
+          uint32_t x = row;
+#pragma unroll
+          for (int p = 0; p < P; p++) x &= ~(R[p] ^ (0u - ((col[p] >> k) & 1u)));
+          const unsigned long long tt = (unsigned long long)row + x + ((cw >> k) & 1u);
+          ncw |= (uint32_t)(tt >> 32) << k;
+          row = (uint32_t)tt | (row ^ x);
+        }
+        const uint32_t v = (j == nb1 - 1) ? vlast : 0xFFFFFFFFu;
+        zc += __popc(~row & v) - __popc(~old & v);
+        line[j * TL] = row;
+        cw = ncw;
+      }
+      i++;
+      if (!score_mode && i < nq && zc + (net2 - 32 * i) < cutoff) {
+        busy = false;
+        state = -1;
+        continue;
+      }
+    }
+    if (i >= nq) {
+      finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, zc, cutoff, L2, net2, qpl, s_list, n_members);
+      busy = false;
+      state = -1;
+    }
+  }
+  flush_align_stats(st, n_pairs, n_members, n_cells);
+}
+
+// ---- dispatch ---------------------------------------------------------------------
+typedef void (*AlignFn)(DevDB, RunBufs, RunParams, int, int);
+
+static AlignFn align_fn(int type, int cls) {
+  if (type == 0) {
+    switch (cls) {
+      case 0: return k_align_win<2, 8>;
+      case 1: return k_align_win<2, 16>;
+      case 2: return k_align_win<2, 24>;
+      case 3: return k_align_win<2, 32>;
+      case 4: return k_align_tiled<2>;
+      default: return k_align_generic<2>;
+    }
+  }
+  switch (cls) {
+    case 0: return k_align_win<5, 8>;
+    case 1: return k_align_win<5, 16>;
+    case 2: return k_align_tiled<5>;
+    default: return k_align_generic<5>;
+  }
+}
+
+// Dynamic shared memory: rep planes | k-mer bitset | (tiled class) row ring.
+static size_t align_smem(int type, int max_nb, int cls) {
+  const int P = type ? 5 : 2;
+  size_t words = (size_t)(((max_nb * P + 3) & ~3) + kListWords);
+  if (cls == tiled_class(type)) words += (size_t)kRingBlocks * kAlignThreads;
+  return 4u * words;
+}
+
+cudaError_t align_configure(int type, int max_nb) {
+  for (int c = 0; c < num_classes(type); c++) {
+    cudaError_t e = cudaFuncSetAttribute((const void *)align_fn(type, c),
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)align_smem(type, max_nb, c));
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+// Resident CTAs per SM of class `cls` (persistent grid = that x SM count).
+int align_occupancy(int type, int cls, int max_nb) {
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)align_fn(type, cls), kAlignThreads,
+                                                    align_smem(type, max_nb, cls)) != cudaSuccess)
+    return 1;
+  return nb < 1 ? 1 : nb;
+}
+
+int align_threads() { return kAlignThreads; }
+
+cudaError_t launch_align(ngia_ctx *c, int cls, cudaStream_t s, int score_mode) {
+  AlignFn fn = align_fn(c->db.type, cls);
+  const size_t smem = align_smem(c->db.type, c->db.max_nb, cls);
+  DevDB db = c->db;
+  RunBufs rb = c->rb;
+  RunParams prm = c->prm;
+  void *args[] = {&db, &rb, &prm, &cls, &score_mode};
+  return cudaLaunchKernel((const void *)fn, dim3(c->grid_align[cls]), dim3(kAlignThreads), args, smem, s);
+}
+
+
+}  // namespace ngia

@@ -1,0 +1,373 @@
+// api.cu — device half of the C ABI (include/ngia.h): context lifetime, the
+// greedy driver in its two forms, and the pair-score entry point.
+//
+// Reference counterparts (CUDA/signalNode/src/func.cu):
+//   ngia_open            readData device copy (104-154)
+//   ngia_cluster_begin   initBench (157-183)
+//   ngia_cluster_step    the while(true) loop of clustering (616-675)
+//   ngia_cluster_end     the cluster[] hand-off to saveResult (692-705)
+//   ngia_close           finish (767-781)
+#include <algorithm>
+#include <climits>
+#include <cstring>
+#include <new>
+
+#include "../host/host_common.h"
+#include "ctx.h"
+
+using ngia::fail;
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) return fail(NGIA_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_));     \
+  } while (0)
+
+namespace {
+
+template <class T>
+cudaError_t dalloc(T **p, size_t count) {
+  return cudaMalloc((void **)p, sizeof(T) * std::max<size_t>(count, 1));
+}
+
+int check_device_error(ngia_ctx *c) {
+  if (c->h_state->err)
+    return fail(NGIA_E_DEVICE, "device error %d in kernel %d (bounded wait expired or scratch too small)",
+                c->h_state->err, c->h_state->err_where);
+  return NGIA_OK;
+}
+
+int pull_state(ngia_ctx *c) {
+  CK(cudaMemcpyAsync(c->h_state, c->rb.st, sizeof(ngia::RunState), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return check_device_error(c);
+}
+
+// One greedy iteration: prepare the representative, filter the unclustered
+// set into class queues, align every class, pick the next representative.
+int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond) {
+  CK(ngia::launch_prep(c, -1));
+  CK(ngia::launch_filter(c));
+  const int nc = ngia::num_classes(c->db.type);
+  if (graph) {
+    // classes run as parallel branches of the body graph
+    CK(cudaEventRecord(c->fork_ev, c->stream));
+    for (int k = 0; k < nc; k++) {
+      CK(cudaStreamWaitEvent(c->side[k], c->fork_ev, 0));
+      CK(ngia::launch_align(c, k, c->side[k], 0));
+      CK(cudaEventRecord(c->join_ev[k], c->side[k]));
+      CK(cudaStreamWaitEvent(c->stream, c->join_ev[k], 0));
+    }
+  } else {
+    for (int k = 0; k < nc; k++) CK(ngia::launch_align(c, k, c->stream, 0));
+  }
+  CK(ngia::launch_next(c, (unsigned long long)cond, graph ? 1 : 0));
+  return NGIA_OK;
+}
+
+void destroy_graph(ngia_ctx *c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = nullptr;
+  c->graph = nullptr;
+  c->graph_ready = false;
+}
+
+// Captures the loop body once into the body of a conditional WHILE node; the
+// node re-runs it until k_next clears the condition.
+int build_graph(ngia_ctx *c) {
+  destroy_graph(c);
+  CK(cudaGraphCreate(&c->graph, 0));
+  cudaGraphConditionalHandle cond;
+  CK(cudaGraphConditionalHandleCreate(&cond, c->graph, 1, cudaGraphCondAssignDefault));
+  cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+  np.conditional.handle = cond;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, c->graph, nullptr, nullptr, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_iteration(c, true, cond);
+  cudaGraph_t captured = nullptr;
+  cudaError_t e = cudaStreamEndCapture(c->stream, &captured);
+  if (rc != NGIA_OK) return rc;
+  if (e != cudaSuccess) return fail(NGIA_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  CK(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
+  c->graph_ready = true;
+  c->graph_prm = c->prm;
+  return NGIA_OK;
+}
+
+bool same_params(const ngia::RunParams &a, const ngia::RunParams &b) {
+  return a.s == b.s && a.w == b.w && a.precise == b.precise && a.word_order == b.word_order;
+}
+
+int validate_params(int type, const ngia_params *p) {
+  if (!p) return fail(NGIA_E_ARG, "null params");
+  if (!(p->similarity >= 0.1f && p->similarity <= 1.0f))
+    return fail(NGIA_E_ARG, "similarity %g outside [0.1, 1.0] (apply ngia_params_clamp)", (double)p->similarity);
+  const int lo = type == 0 ? 4 : 2, hi = type == 0 ? 8 : 3;
+  if (p->word_length < lo || p->word_length > hi)
+    return fail(NGIA_E_ARG, "word length %d outside [%d, %d] (apply ngia_params_clamp)", p->word_length, lo, hi);
+  if (p->precise != 0 && p->precise != 1) return fail(NGIA_E_ARG, "precise must be 0 or 1");
+  return NGIA_OK;
+}
+
+}  // namespace
+
+extern "C" int ngia_open(const ngia_db_view *v, ngia_ctx **out) {
+  ngia::clear_error();
+  if (!v || !out) return fail(NGIA_E_ARG, "ngia_open: null argument");
+  if (v->n <= 0 || (v->type != 0 && v->type != 1) || !v->words || !v->rec_off || v->n_words <= 0)
+    return fail(NGIA_E_ARG, "ngia_open: empty or malformed database view (n=%d type=%d)", v->n, v->type);
+  ngia_ctx *c = new (std::nothrow) ngia_ctx();
+  if (!c) return fail(NGIA_E_NOMEM, "ngia_open: out of host memory");
+  *out = nullptr;
+  int rc = NGIA_OK;
+  auto bail = [&](int r) {
+    ngia_close(c);
+    return r;
+  };
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) return bail(fail(NGIA_E_CUDA, "no CUDA device: %s", cudaGetErrorString(e)));
+  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
+    return bail(fail(NGIA_E_CUDA, "cannot query SM count"));
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(NGIA_E_CUDA, "cannot create stream"));
+  for (int k = 0; k < ngia::kNumClasses; k++) {
+    if (cudaStreamCreateWithFlags(&c->side[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return bail(fail(NGIA_E_CUDA, "cannot create side streams"));
+  }
+  if (cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess)
+    return bail(fail(NGIA_E_CUDA, "cannot create event"));
+  const int64_t n = v->n;
+  const int type = v->type;
+  const int A = ngia::count_words(type);
+  c->n_words = v->n_words;
+  c->longest = v->longest;
+  // database: one host-to-device copy of the packed records and offsets
+  if (dalloc(&c->d_words, (size_t)v->n_words + 4) != cudaSuccess || dalloc(&c->d_off, (size_t)n) != cudaSuccess ||
+      dalloc(&c->d_len, (size_t)n) != cudaSuccess || dalloc(&c->d_net, (size_t)n) != cudaSuccess ||
+      dalloc(&c->d_cnt, (size_t)n * A) != cudaSuccess)
+    return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation of the database failed"));
+  e = cudaMemcpyAsync(c->d_words, v->words, sizeof(uint32_t) * (size_t)v->n_words, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->d_off, v->rec_off, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) return bail(fail(NGIA_E_CUDA, "ngia_open: copy: %s", cudaGetErrorString(e)));
+  int32_t *d_flags = nullptr;
+  if (dalloc(&d_flags, 3) != cudaSuccess) return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation failed"));
+  cudaMemsetAsync(d_flags, 0, 3 * sizeof(int32_t), c->stream);
+  c->db.words = c->d_words;
+  c->db.off = c->d_off;
+  c->db.len = c->d_len;
+  c->db.net = c->d_net;
+  c->db.cnt = c->d_cnt;
+  c->db.n = (int32_t)n;
+  c->db.type = type;
+  c->db.hw = ngia::header_words(type);
+  c->db.P = ngia::plane_count(type);
+  c->db.A = A;
+  e = ngia::launch_loader(c, d_flags, d_flags + 1, d_flags + 2);
+  int32_t h_flags[3] = {0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h_flags, d_flags, sizeof(h_flags), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  cudaFree(d_flags);
+  if (e != cudaSuccess) return bail(fail(NGIA_E_CUDA, "ngia_open: loader: %s", cudaGetErrorString(e)));
+  if (h_flags[2]) return bail(fail(NGIA_E_FORMAT, "ngia_open: a record offset or header is out of range"));
+  c->db.max_nb = std::max(1, h_flags[0]);
+  c->db.has_short = h_flags[1];
+  // run buffers
+  const size_t nbw = (size_t)(n + 31) / 32;
+  ngia::RunBufs &rb = c->rb;
+  bool ok = dalloc(&rb.st, 1) == cudaSuccess && dalloc(&rb.cluster, (size_t)n) == cudaSuccess &&
+            dalloc(&rb.ident, (size_t)n) == cudaSuccess && dalloc(&rb.alive, nbw) == cudaSuccess &&
+            dalloc(&rb.rep_rec, 32 + (size_t)ngia::kMaxBlocks * 5 + 64) == cudaSuccess &&
+            dalloc(&rb.rep_list, ngia::kListWords) == cudaSuccess &&
+            dalloc(&rb.first_short, ngia::kRefGridThreads) == cudaSuccess &&
+            dalloc(&rb.scan_part, nbw) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&rb.flags, 4 * std::max<size_t>(nbw, 1)) == cudaSuccess;
+  for (int k = 0; ok && k < ngia::num_classes(type); k++) ok = dalloc(&rb.queue[k], (size_t)n) == cudaSuccess;
+  if (!ok) return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation of run buffers failed"));
+  cudaMemsetAsync(rb.rep_list, 0, 4 * ngia::kListWords, c->stream);
+  // launch shapes
+  if (ngia::align_configure(type, c->db.max_nb) != cudaSuccess)
+    return bail(fail(NGIA_E_CUDA, "ngia_open: kernel attributes"));
+  for (int k = 0; k < ngia::num_classes(type); k++)
+    c->grid_align[k] = c->num_sms * ngia::align_occupancy(type, k, c->db.max_nb);
+  c->grid_filter = c->num_sms * 8;
+  const int g = ngia::generic_class(type);
+  rb.generic_lanes = c->grid_align[g] * ngia::align_threads();
+  rb.scratch_words = (int64_t)rb.generic_lanes * c->db.max_nb;
+  if (dalloc(&rb.scratch, (size_t)rb.scratch_words) != cudaSuccess)
+    return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation of alignment scratch failed"));
+  if (cudaMallocHost((void **)&c->h_state, sizeof(ngia::RunState)) != cudaSuccess)
+    return bail(fail(NGIA_E_NOMEM, "ngia_open: pinned allocation failed"));
+  std::memset(c->h_state, 0, sizeof(ngia::RunState));
+  e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return bail(fail(NGIA_E_CUDA, "ngia_open: %s", cudaGetErrorString(e)));
+  (void)rc;
+  *out = c;
+  return NGIA_OK;
+}
+
+extern "C" int ngia_close(ngia_ctx *c) {
+  if (!c) return NGIA_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  destroy_graph(c);
+  cudaFree(c->d_words);
+  cudaFree(c->d_off);
+  cudaFree(c->d_len);
+  cudaFree(c->d_net);
+  cudaFree(c->d_cnt);
+  ngia::RunBufs &rb = c->rb;
+  cudaFree(rb.st);
+  cudaFree(rb.cluster);
+  cudaFree(rb.ident);
+  cudaFree(rb.alive);
+  cudaFree(rb.rep_rec);
+  cudaFree(rb.rep_list);
+  cudaFree(rb.first_short);
+  cudaFree(rb.scan_part);
+  cudaFree(rb.flags);
+  cudaFree(rb.scratch);
+  for (int k = 0; k < ngia::kNumClasses; k++) cudaFree(rb.queue[k]);
+  if (c->h_state) cudaFreeHost(c->h_state);
+  for (int k = 0; k < ngia::kNumClasses; k++) {
+    if (c->side[k]) cudaStreamDestroy(c->side[k]);
+    if (c->join_ev[k]) cudaEventDestroy(c->join_ev[k]);
+  }
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return NGIA_OK;
+}
+
+extern "C" void *ngia_stream(ngia_ctx *c) { return c ? (void *)c->stream : nullptr; }
+
+extern "C" int ngia_device_count(int32_t *count) {
+  if (!count) return fail(NGIA_E_ARG, "ngia_device_count: null argument");
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) n = 0;
+  *count = n;
+  return NGIA_OK;
+}
+
+extern "C" int ngia_cluster_begin(ngia_ctx *c, const ngia_params *p, int32_t mode) {
+  ngia::clear_error();
+  if (!c) return fail(NGIA_E_ARG, "ngia_cluster_begin: null context");
+  int rc = validate_params(c->db.type, p);
+  if (rc) return rc;
+  if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH) return fail(NGIA_E_ARG, "unknown mode %d", mode);
+  c->prm.s = p->similarity;
+  c->prm.w = p->word_length;
+  c->prm.precise = p->precise;
+  c->prm.word_order = 0;
+  if (const char *wo = getenv("NGIA_WORD_ORDER")) c->prm.word_order = atoi(wo);
+  if (c->db.has_short && !c->prm.precise) c->prm.word_order = 1;  // exact path is word first
+  c->mode = mode;
+  CK(ngia::launch_init_run(c));
+  rc = pull_state(c);
+  if (rc) return rc;
+  if (mode == NGIA_MODE_GRAPH && !(c->graph_ready && same_params(c->graph_prm, c->prm))) {
+    rc = build_graph(c);
+    if (rc) return rc;
+  }
+  c->begun = true;
+  return NGIA_OK;
+}
+
+extern "C" int ngia_cluster_step(ngia_ctx *c, int64_t max_iters, int32_t *done) {
+  if (!c) return fail(NGIA_E_ARG, "ngia_cluster_step: null context");
+  if (!c->begun) return fail(NGIA_E_STATE, "ngia_cluster_step before ngia_cluster_begin");
+  if (c->h_state->done) {
+    if (done) *done = 1;
+    return NGIA_OK;
+  }
+  if (c->mode == NGIA_MODE_GRAPH) {
+    c->h_state->iter_limit = max_iters > 0 ? c->h_state->iter + max_iters : LLONG_MAX;
+    CK(cudaMemcpyAsync(&c->rb.st->iter_limit, &c->h_state->iter_limit, sizeof(int64_t), cudaMemcpyHostToDevice,
+                       c->stream));
+    CK(cudaGraphLaunch(c->graph_exec, c->stream));
+    int rc = pull_state(c);
+    if (rc) return rc;
+  } else {
+    for (int64_t it = 0; max_iters <= 0 || it < max_iters; it++) {
+      int rc = enqueue_iteration(c, false, 0);
+      if (rc) return rc;
+      rc = pull_state(c);  // the per-representative host round trip of the plain form
+      if (rc) return rc;
+      if (c->h_state->done) break;
+    }
+  }
+  if (done) *done = c->h_state->done;
+  return NGIA_OK;
+}
+
+extern "C" int ngia_cluster_end(ngia_ctx *c, int32_t *cluster_out, int32_t *identity_out, ngia_stats *stats) {
+  if (!c) return fail(NGIA_E_ARG, "ngia_cluster_end: null context");
+  if (!c->begun) return fail(NGIA_E_STATE, "ngia_cluster_end before ngia_cluster_begin");
+  const size_t n = (size_t)c->db.n;
+  if (cluster_out) CK(cudaMemcpyAsync(cluster_out, c->rb.cluster, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  if (identity_out) CK(cudaMemcpyAsync(identity_out, c->rb.ident, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  int rc = pull_state(c);
+  if (rc) return rc;
+  if (stats) {
+    const ngia::RunState &s = *c->h_state;
+    stats->iterations = s.iter;
+    stats->candidates = (int64_t)s.st_candidates;
+    stats->base_pass = (int64_t)s.st_base_pass;
+    stats->align_pairs = (int64_t)s.st_align_pairs;
+    stats->members = (int64_t)s.st_members;
+    stats->band_cells = (int64_t)s.st_band_cells;
+    stats->filter_bytes = (int64_t)s.st_filter_bytes;
+    stats->word_checks = (int64_t)s.st_word_checks;
+  }
+  return NGIA_OK;
+}
+
+extern "C" int ngia_cluster(ngia_ctx *c, const ngia_params *p, int32_t mode, int32_t *cluster_out,
+                            int32_t *identity_out, ngia_stats *stats) {
+  int rc = ngia_cluster_begin(c, p, mode);
+  if (rc) return rc;
+  int32_t done = 0;
+  rc = ngia_cluster_step(c, 0, &done);
+  if (rc) return rc;
+  if (!done) return fail(NGIA_E_STATE, "clustering stopped before every sequence was assigned");
+  return ngia_cluster_end(c, cluster_out, identity_out, stats);
+}
+
+extern "C" int ngia_pair_scores(ngia_ctx *c, const ngia_params *p, int32_t rep, const int32_t *cands, int32_t n,
+                                int32_t *out) {
+  ngia::clear_error();
+  if (!c || !cands || !out || n < 0) return fail(NGIA_E_ARG, "ngia_pair_scores: bad argument");
+  int rc = validate_params(c->db.type, p);
+  if (rc) return rc;
+  if (rep < 0 || rep >= c->db.n) return fail(NGIA_E_ARG, "ngia_pair_scores: rep %d out of range", rep);
+  for (int32_t k = 0; k < n; k++)
+    if (cands[k] < 0 || cands[k] >= c->db.n) return fail(NGIA_E_ARG, "ngia_pair_scores: candidate out of range");
+  if (n == 0) return NGIA_OK;
+  if (n > c->db.n) return fail(NGIA_E_LIMIT, "ngia_pair_scores: at most n pairs per call");
+  c->prm.s = p->similarity;
+  c->prm.w = p->word_length;
+  c->prm.precise = p->precise;
+  int32_t *d_c = nullptr, *d_o = nullptr;
+  CK(dalloc(&d_c, (size_t)n));
+  CK(dalloc(&d_o, 4 * (size_t)n));
+  c->rb.score_cands = d_c;
+  c->rb.score_out = d_o;
+  CK(cudaMemcpyAsync(d_c, cands, 4 * (size_t)n, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaMemsetAsync(c->rb.st, 0, sizeof(ngia::RunState), c->stream));
+  CK(ngia::launch_prep(c, rep));
+  CK(ngia::launch_score_classify(c, n));
+  for (int k = 0; k < ngia::num_classes(c->db.type); k++) CK(ngia::launch_align(c, k, c->stream, 1));
+  CK(cudaMemcpyAsync(out, d_o, 16 * (size_t)n, cudaMemcpyDeviceToHost, c->stream));
+  rc = pull_state(c);
+  cudaFree(d_c);
+  cudaFree(d_o);
+  c->rb.score_cands = nullptr;
+  c->rb.score_out = nullptr;
+  c->begun = false;
+  return rc;
+}

@@ -1,0 +1,52 @@
+// ctx.h — the library context behind the opaque ngia_ctx handle and the
+// host-side launchers each kernel translation unit provides.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "../../include/ngia.h"
+#include "common.cuh"
+
+struct ngia_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  ngia::DevDB db{};
+  // owned device allocations of the database
+  uint32_t *d_words = nullptr;
+  int64_t *d_off = nullptr;
+  int32_t *d_len = nullptr, *d_net = nullptr;
+  uint32_t *d_cnt = nullptr;
+  int64_t n_words = 0;
+  int32_t longest = 0;
+  // run buffers
+  ngia::RunBufs rb{};
+  ngia::RunState *h_state = nullptr;  // pinned mirror
+  ngia::RunParams prm{};
+  int mode = 0;
+  bool begun = false;
+  // launch shapes
+  int grid_filter = 0;
+  int grid_align[ngia::kNumClasses] = {0};
+  // graph form of the greedy loop
+  cudaGraphExec_t graph_exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  bool graph_ready = false;
+  ngia::RunParams graph_prm{};
+  cudaStream_t side[ngia::kNumClasses] = {nullptr};
+  cudaEvent_t fork_ev = nullptr, join_ev[ngia::kNumClasses] = {nullptr};
+};
+
+namespace ngia {
+// loader.cu / filter.cu
+cudaError_t launch_loader(ngia_ctx *c, int32_t *d_maxnb, int32_t *d_short, int32_t *d_bad);
+cudaError_t launch_init_run(ngia_ctx *c);
+cudaError_t launch_prep(ngia_ctx *c, int score_rep);
+cudaError_t launch_filter(ngia_ctx *c);
+cudaError_t launch_next(ngia_ctx *c, unsigned long long cond_handle, int use_cond);
+cudaError_t launch_score_classify(ngia_ctx *c, int n);
+// align.cu
+cudaError_t launch_align(ngia_ctx *c, int cls, cudaStream_t s, int score_mode);
+int align_occupancy(int type, int cls, int max_nb);
+int align_threads();
+cudaError_t align_configure(int type, int max_nb);
+}  // namespace ngia

@@ -1,0 +1,283 @@
+"""Python binding of libngia (include/ngia.h) over ctypes.
+
+The library is the product; this module only marshals arguments.  It loads
+``_build/libngia.so`` next to this file and raises if it is missing (there is
+no fallback implementation).  Arrays cross the boundary as numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libngia.so"
+
+MODE_PLAIN = 0
+MODE_GRAPH = 1
+
+
+class NgiaError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ngia error {code}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("similarity", C.c_float), ("word_length", C.c_int32), ("precise", C.c_int32)]
+
+
+class DBView(C.Structure):
+    _fields_ = [("n", C.c_int32), ("type", C.c_int32), ("longest", C.c_int32), ("shortest", C.c_int32),
+                ("words", C.POINTER(C.c_uint32)), ("n_words", C.c_int64), ("rec_off", C.POINTER(C.c_int64))]
+
+
+class DBHost(C.Structure):
+    _fields_ = [("view", DBView), ("name_len", C.POINTER(C.c_int32)), ("read_len", C.POINTER(C.c_int32)),
+                ("fasta_off", C.POINTER(C.c_int64)), ("pack_off", C.POINTER(C.c_int64))]
+
+
+class SynthParams(C.Structure):
+    _fields_ = [("type", C.c_int32), ("len_dist", C.c_int32), ("n_seqs", C.c_int64), ("n_ancestors", C.c_int32),
+                ("len_min", C.c_int32), ("len_max", C.c_int32), ("len_a", C.c_double), ("len_b", C.c_double),
+                ("subst_max", C.c_double), ("indel_frac", C.c_double), ("indel_max", C.c_int32),
+                ("novel_frac", C.c_double), ("seed", C.c_uint64)]
+
+
+class Stats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("iterations", "candidates", "base_pass", "align_pairs", "members",
+                                         "band_cells", "filter_bytes", "word_checks")]
+
+    def as_dict(self) -> dict:
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libngia.so (built by build_native.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+    L = C.CDLL(str(LIB_PATH))
+    P, I32, I64, VP = C.POINTER, C.c_int32, C.c_int64, C.c_void_p
+    sig = {
+        "ngia_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+        "ngia_version": (C.c_char_p, []),
+        "ngia_free": (None, [VP]),
+        "ngia_params_clamp": (C.c_int, [I32, P(Params)]),
+        "ngia_db_load": (C.c_int, [C.c_char_p, P(P(DBHost))]),
+        "ngia_db_pack": (C.c_int, [I32, C.c_char_p, P(I64), I64, P(I32), P(P(DBHost))]),
+        "ngia_makedb": (C.c_int, [C.c_char_p, C.c_char_p, I32]),
+        "ngia_save_result": (C.c_int, [C.c_char_p, C.c_char_p, P(DBHost), P(I32), P(I32)]),
+        "ngia_db_free": (None, [P(DBHost)]),
+        "ngia_synth_generate": (C.c_int, [P(SynthParams), P(VP), P(P(I64)), P(I64)]),
+        "ngia_write_fasta": (C.c_int, [C.c_char_p, C.c_char_p, P(I64), I64, I32]),
+        "ngia_open": (C.c_int, [P(DBView), P(VP)]),
+        "ngia_cluster": (C.c_int, [VP, P(Params), I32, P(I32), P(I32), P(Stats)]),
+        "ngia_cluster_begin": (C.c_int, [VP, P(Params), I32]),
+        "ngia_cluster_step": (C.c_int, [VP, I64, P(I32)]),
+        "ngia_cluster_end": (C.c_int, [VP, P(I32), P(I32), P(Stats)]),
+        "ngia_pair_scores": (C.c_int, [VP, P(Params), I32, P(I32), I32, P(I32)]),
+        "ngia_stream": (VP, [VP]),
+        "ngia_device_count": (C.c_int, [P(I32)]),
+        "ngia_close": (C.c_int, [VP]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        buf = C.create_string_buffer(512)
+        lib().ngia_last_error(buf, 512)
+        raise NgiaError(rc, buf.value.decode(errors="replace"))
+
+
+def _i32p(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def _i64p(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def device_count() -> int:
+    n = C.c_int32()
+    _check(lib().ngia_device_count(C.byref(n)))
+    return n.value
+
+
+def params_clamp(db_type: int, similarity: float, word_length: int, precise: int = 0) -> Params:
+    p = Params(similarity, word_length, precise)
+    _check(lib().ngia_params_clamp(db_type, C.byref(p)))
+    return p
+
+
+# ---- synthetic workloads (the five BASELINE configurations) -----------------
+CONFIGS = {
+    # 20,000 DNA from 400 ancestors, N(1450, 80) clipped [1200, 1700]
+    "dna_small": dict(type=0, len_dist=0, n_seqs=20000, n_ancestors=400, len_a=1450.0, len_b=80.0,
+                      len_min=1200, len_max=1700, subst_max=0.20, indel_frac=0.05, indel_max=3),
+    # 1,000,000 DNA from 20,000 ancestors, N(1450, 120) clipped [900, 2000]
+    "dna_1m": dict(type=0, len_dist=0, n_seqs=1000000, n_ancestors=20000, len_a=1450.0, len_b=120.0,
+                   len_min=900, len_max=2000, subst_max=0.20, indel_frac=0.05, indel_max=3),
+    # 200,000 proteins from 8,000 ancestors, lognormal(median 380, sigma 0.7) clipped [20, 35000]
+    "protein_200k": dict(type=1, len_dist=1, n_seqs=200000, n_ancestors=8000, len_a=380.0, len_b=0.7,
+                         len_min=20, len_max=35000, subst_max=0.50, indel_frac=0.05, indel_max=5),
+}
+
+
+def synth(type: int = 0, n_seqs: int = 1000, n_ancestors: int = 20, len_dist: int = 0, len_a: float = 1450.0,
+          len_b: float = 80.0, len_min: int = 1200, len_max: int = 1700, subst_max: float = 0.2,
+          indel_frac: float = 0.05, indel_max: int = 3, novel_frac: float = 0.0, seed: int = 1):
+    """Generates sequences; returns (bytes of all residues, int64 offsets[n+1])."""
+    p = SynthParams(type, len_dist, n_seqs, n_ancestors, len_min, len_max, len_a, len_b, subst_max, indel_frac,
+                    indel_max, novel_frac, seed)
+    seq = C.c_void_p()
+    off = C.POINTER(C.c_int64)()
+    n = C.c_int64()
+    _check(lib().ngia_synth_generate(C.byref(p), C.byref(seq), C.byref(off), C.byref(n)))
+    try:
+        offs = np.ctypeslib.as_array(off, shape=(n.value + 1,)).copy()
+        data = C.string_at(seq, int(offs[-1]))
+    finally:
+        lib().ngia_free(seq)
+        lib().ngia_free(C.cast(off, C.c_void_p))
+    return data, offs
+
+
+def write_fasta(path: str, seq: bytes, off: np.ndarray, width: int = 80) -> None:
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    _check(lib().ngia_write_fasta(str(path).encode(), seq, _i64p(off), len(off) - 1, width))
+
+
+class DB:
+    """A makeDB database in host memory (owned by the library)."""
+
+    def __init__(self, ptr):
+        self._ptr = ptr
+        h = ptr.contents
+        v = h.view
+        self.n, self.type, self.longest, self.shortest = v.n, v.type, v.longest, v.shortest
+        self.words = np.ctypeslib.as_array(v.words, shape=(v.n_words,))
+        self.rec_off = np.ctypeslib.as_array(v.rec_off, shape=(v.n,))
+        self.read_len = np.ctypeslib.as_array(h.read_len, shape=(v.n,))
+        self.name_len = np.ctypeslib.as_array(h.name_len, shape=(v.n,))
+        self.fasta_off = np.ctypeslib.as_array(h.fasta_off, shape=(v.n,))
+        self.pack_off = np.ctypeslib.as_array(h.pack_off, shape=(v.n,))
+
+    @property
+    def view(self) -> DBView:
+        return self._ptr.contents.view
+
+    @classmethod
+    def load(cls, dirpath: str) -> "DB":
+        p = C.POINTER(DBHost)()
+        _check(lib().ngia_db_load(str(dirpath).encode(), C.byref(p)))
+        return cls(p)
+
+    @classmethod
+    def pack(cls, db_type: int, seq: bytes, off: np.ndarray) -> "DB":
+        off = np.ascontiguousarray(off, dtype=np.int64)
+        p = C.POINTER(DBHost)()
+        _check(lib().ngia_db_pack(db_type, seq, _i64p(off), len(off) - 1, None, C.byref(p)))
+        return cls(p)
+
+    def record(self, i: int) -> np.ndarray:
+        o = int(self.rec_off[i])
+        hw = 6 if self.type == 0 else 30
+        P = 2 if self.type == 0 else 5
+        L = int(self.words[o])
+        return self.words[o:o + hw + (L + 31) // 32 * P]
+
+    def save_result(self, dbdir: str, outdir: str, cluster: np.ndarray) -> int:
+        cl = np.ascontiguousarray(cluster, dtype=np.int32)
+        nc = C.c_int32()
+        _check(lib().ngia_save_result(str(dbdir).encode(), str(outdir).encode(), self._ptr, _i32p(cl),
+                                      C.byref(nc)))
+        return nc.value
+
+    def close(self) -> None:
+        if self._ptr:
+            lib().ngia_db_free(self._ptr)
+            self._ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def makedb(fasta: str, outdir: str, db_type: int) -> None:
+    _check(lib().ngia_makedb(str(fasta).encode(), str(outdir).encode(), db_type))
+
+
+class Context:
+    """Device context: the database resident in HBM plus run buffers."""
+
+    def __init__(self, db: DB):
+        self.db = db
+        self._h = C.c_void_p()
+        _check(lib().ngia_open(C.byref(db.view), C.byref(self._h)))
+
+    def cluster(self, params: Params, mode: int = MODE_GRAPH):
+        n = self.db.n
+        cl = np.empty(n, dtype=np.int32)
+        ident = np.empty(n, dtype=np.int32)
+        st = Stats()
+        _check(lib().ngia_cluster(self._h, C.byref(params), mode, _i32p(cl), _i32p(ident), C.byref(st)))
+        return cl, ident, st.as_dict()
+
+    def begin(self, params: Params, mode: int = MODE_GRAPH) -> None:
+        _check(lib().ngia_cluster_begin(self._h, C.byref(params), mode))
+
+    def step(self, max_iters: int) -> bool:
+        done = C.c_int32()
+        _check(lib().ngia_cluster_step(self._h, max_iters, C.byref(done)))
+        return bool(done.value)
+
+    def end(self):
+        n = self.db.n
+        cl = np.empty(n, dtype=np.int32)
+        ident = np.empty(n, dtype=np.int32)
+        st = Stats()
+        _check(lib().ngia_cluster_end(self._h, _i32p(cl), _i32p(ident), C.byref(st)))
+        return cl, ident, st.as_dict()
+
+    def pair_scores(self, params: Params, rep: int, cands) -> np.ndarray:
+        c = np.ascontiguousarray(cands, dtype=np.int32)
+        out = np.empty((len(c), 4), dtype=np.int32)
+        _check(lib().ngia_pair_scores(self._h, C.byref(params), rep, _i32p(c), len(c), _i32p(out)))
+        return out
+
+    @property
+    def stream(self) -> int:
+        return lib().ngia_stream(self._h) or 0
+
+    def close(self) -> None:
+        if self._h:
+            lib().ngia_close(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,67 @@
+/*
+ * ngia_oracle.h — CPU restatement of nGIA's single-node clustering
+ * (CUDA/signalNode/src/func.cu) used as the parity checker and the timed CPU
+ * baseline.  TEST INFRASTRUCTURE ONLY: the product library never links,
+ * loads or calls it.
+ */
+#ifndef NGIA_ORACLE_H
+#define NGIA_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct ora_db {
+  int32_t n, longest, shortest, type;
+  int32_t *name_len, *read_len;
+  int64_t *fasta_off, *pack_off;
+  int64_t *offsets;   /* word offset of record i in buf (func.cu:117-124) */
+  uint32_t *buf;      /* records                                          */
+  int64_t buf_words;
+} ora_db;
+
+/* stats[] slots filled by ora_cluster */
+enum {
+  ORA_ITER = 0,      /* representatives                                   */
+  ORA_CAND,          /* (rep, candidate) visits = base-filter jobs        */
+  ORA_BASE_PASS,     /* base-filter survivors                             */
+  ORA_WORD_EVAL,     /* word-filter jobs that were evaluated (not skipped) */
+  ORA_WORD_PASS,     /* word-filter survivors = alignment jobs            */
+  ORA_MEMBERS,       /* alignment survivors (members incl. reps)          */
+  ORA_CELLS,         /* band cells of the alignment jobs                  */
+  ORA_FILTER_BYTES,  /* header bytes of every job + planes of word jobs   */
+  ORA_NSTATS
+};
+
+int  ora_load(const char *dir, ora_db *db);
+void ora_free(ora_db *db);
+void ora_clamp(int type, float *s, int *w, int *precise);
+
+/* Greedy clustering of func.cu:607-677.  cluster[n], identity[n] out;
+ * stats[ORA_NSTATS] out (may be NULL).  max_iters > 0 stops after that many
+ * representatives (cluster[] then holds -1 for unassigned sequences).
+ * nthreads <= 0 uses all OpenMP threads.  Returns the iteration count. */
+int64_t ora_cluster(const uint32_t *buf, const int64_t *offsets, int n, int type,
+                    float s, int w, int precise, int nthreads, int64_t max_iters,
+                    int32_t *cluster, int32_t *identity, int64_t *stats);
+
+/* Per-pair stage values (rep, cand): out[0] composition sum, out[1]
+ * short-word count (-1 if a net length < 16 skips the filter), out[2]
+ * banded-LCS score, out[3] block band; out[4..6] = pass flags of the three
+ * stages; out[7] = band cells. */
+void ora_pair(const uint32_t *buf, const int64_t *offsets, int type, float s, int w,
+              int rep, int cand, int32_t *out);
+
+/* The reference's per-pair alignment on raw records (rep, query). */
+int ora_dp_sum(const uint32_t *rep, const uint32_t *query, int type, float s,
+               int *band, int64_t *cells);
+
+/* saveResult (func.cu:680-764): writes cluster.txt and represent.fasta. */
+int ora_save(const char *dbdir, const char *outdir, const ora_db *db, const int32_t *cluster,
+             int32_t *n_clusters);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

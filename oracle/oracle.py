@@ -1,0 +1,82 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the CPU
+baseline leg of bench.py as the checker; the product never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "_build" / "liboracle.so"
+NSTATS = 8
+STAT_NAMES = ["iterations", "candidates", "base_pass", "word_eval", "word_pass", "members", "cells",
+              "filter_bytes"]
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB.exists():
+            raise ImportError(f"{LIB} is missing: build it with oracle/build_oracle.py")
+        L = C.CDLL(str(LIB))
+        P = C.POINTER
+        L.ora_cluster.restype = C.c_int64
+        L.ora_cluster.argtypes = [P(C.c_uint32), P(C.c_int64), C.c_int, C.c_int, C.c_float, C.c_int, C.c_int,
+                                  C.c_int, C.c_int64, P(C.c_int32), P(C.c_int32), P(C.c_int64)]
+        L.ora_pair.restype = None
+        L.ora_pair.argtypes = [P(C.c_uint32), P(C.c_int64), C.c_int, C.c_float, C.c_int, C.c_int, C.c_int,
+                               P(C.c_int32)]
+        L.ora_clamp.restype = None
+        L.ora_clamp.argtypes = [C.c_int, P(C.c_float), P(C.c_int), P(C.c_int)]
+        L.ora_dp_sum.restype = C.c_int
+        L.ora_dp_sum.argtypes = [P(C.c_uint32), P(C.c_uint32), C.c_int, C.c_float, P(C.c_int), P(C.c_int64)]
+        _lib = L
+    return _lib
+
+
+def clamp(db_type: int, s: float, w: int, precise: int = 0):
+    sf, wi, pi = C.c_float(s), C.c_int(w), C.c_int(precise)
+    lib().ora_clamp(db_type, C.byref(sf), C.byref(wi), C.byref(pi))
+    return sf.value, wi.value, pi.value
+
+
+def cluster(words: np.ndarray, rec_off: np.ndarray, db_type: int, s: float, w: int, precise: int = 0,
+            threads: int = 0, max_iters: int = 0):
+    """Clusters with already-clamped parameters; returns (cluster, identity, stats)."""
+    words = np.ascontiguousarray(words, dtype=np.uint32)
+    rec_off = np.ascontiguousarray(rec_off, dtype=np.int64)
+    n = len(rec_off)
+    cl = np.empty(n, dtype=np.int32)
+    ident = np.empty(n, dtype=np.int32)
+    st = np.zeros(NSTATS, dtype=np.int64)
+    lib().ora_cluster(words.ctypes.data_as(C.POINTER(C.c_uint32)), rec_off.ctypes.data_as(C.POINTER(C.c_int64)),
+                      n, db_type, C.c_float(s), w, precise, threads, max_iters,
+                      cl.ctypes.data_as(C.POINTER(C.c_int32)), ident.ctypes.data_as(C.POINTER(C.c_int32)),
+                      st.ctypes.data_as(C.POINTER(C.c_int64)))
+    return cl, ident, dict(zip(STAT_NAMES, (int(x) for x in st)))
+
+
+def pair(words: np.ndarray, rec_off: np.ndarray, db_type: int, s: float, w: int, rep: int, cand: int):
+    """(composition sum, word count or -1, dp score, band, base ok, word ok, dp ok, band cells)."""
+    words = np.ascontiguousarray(words, dtype=np.uint32)
+    rec_off = np.ascontiguousarray(rec_off, dtype=np.int64)
+    out = np.zeros(8, dtype=np.int32)
+    lib().ora_pair(words.ctypes.data_as(C.POINTER(C.c_uint32)), rec_off.ctypes.data_as(C.POINTER(C.c_int64)),
+                   db_type, C.c_float(s), w, rep, cand, out.ctypes.data_as(C.POINTER(C.c_int32)))
+    return out
+
+
+def dp_sum(rep_rec: np.ndarray, query_rec: np.ndarray, db_type: int, s: float):
+    """Alignment score of two raw records; returns (score, band, cells)."""
+    r = np.ascontiguousarray(rep_rec, dtype=np.uint32)
+    q = np.ascontiguousarray(query_rec, dtype=np.uint32)
+    band, cells = C.c_int(), C.c_int64()
+    sc = lib().ora_dp_sum(r.ctypes.data_as(C.POINTER(C.c_uint32)), q.ctypes.data_as(C.POINTER(C.c_uint32)),
+                          db_type, C.c_float(s), C.byref(band), C.byref(cells))
+    return sc, band.value, cells.value
