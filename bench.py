@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark of the greedy clustering hot path on GB300.
+
+Workload: the 1,000,000-sequence DNA configuration (20,000 ancestors, lengths
+Normal(1450, 120) clipped to [900, 2000], substitutions U[0, 0.20], indels
+1-3 at 5% of that rate), similarity 0.85, word length 5; generated in memory
+by the seeded generator (no public dataset).  One step = S greedy iterations
+(each: longest unclustered sequence becomes the representative, every
+unclustered sequence is filtered and aligned against it, members join) run by
+the device-side driver; the run continues from step to step.
+
+value  = candidate sequences screened per second (sum over the timed
+         iterations of the unclustered-set size), device time from CUDA events
+         on the library's stream, max over ranks, summed over ranks.
+e2e    = the same metric through the C ABI with host buffers: per step
+         ngia_open (database host-to-device from pinned memory), S iterations,
+         results device-to-host, close.
+Multi-GPU: independent replicas (the path has no exchange step on one node).
+
+`--impl reference` times the reference algorithm's CPU restatement (the
+oracle; the reference's own CPU path is a SYCL build that cannot be compiled
+here) on the host cores, one greedy iteration per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "ngia-metax_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "seqs/sec (candidate sequences screened by the greedy clustering loop, bit-exact)"
+UNIT = "candidate seqs/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--iters-per-step", type=int, default=32)
+    ap.add_argument("--similarity", type=float, default=0.85)
+    ap.add_argument("--word", type=int, default=5)
+    ap.add_argument("--workload", default="dna_1m")
+    ap.add_argument("--n-seqs", type=int, default=0, help="override the sequence count (testing only)")
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--mode", default="graph", choices=["graph", "plain"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--skip-e2e", action="store_true")
+    ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--cpu-only", action="store_true", help="no GPU at all (tests of the replica logic)")
+    return ap.parse_args()
+
+
+# ---- distributed replicas ------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def reduce(self, value: float, op: str) -> float:
+        if not self.pg:
+            return value
+        import torch
+
+        t = torch.tensor([value], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX if op == "max" else self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---- clocks during the timed region -----------------------------------------------
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict | None:
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                try:
+                    rows.append((float(f[1]), float(f[2]), float(f[3]), f[5:9]))
+                except ValueError:
+                    pass
+        os.unlink(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k, v in enumerate(r[3]) if v.lower().startswith("active")})
+        load = [r for r in rows if r[2] > 200.0] or rows
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "of measured"}
+    return {"hbm_gbs": 6800.0, "source": "of fallback"}
+
+
+def make_db(args):
+    import ngia
+
+    cfg = dict(ngia.CONFIGS[args.workload])
+    if args.n_seqs:
+        cfg["n_seqs"] = args.n_seqs
+    seqs = ngia.synth(**cfg, seed=args.seed)
+    db = ngia.DB.pack(cfg["type"], seqs, seqs.off)
+    seqs.close()
+    return db, cfg
+
+
+def workload_desc(args, cfg) -> dict:
+    return {"workload": f"{args.workload}: {cfg['n_seqs']:,} {'DNA' if cfg['type'] == 0 else 'protein'} "
+                        f"sequences, {cfg['n_ancestors']:,} ancestors, lengths ~N({cfg['len_a']:.0f},"
+                        f"{cfg['len_b']:.0f}) clipped [{cfg['len_min']},{cfg['len_max']}], s={args.similarity},"
+                        f" w={args.word}",
+            "iters_per_step": args.iters_per_step, "similarity": args.similarity, "word_length": args.word,
+            "driver": args.mode, "seed": args.seed,
+            "l2": "inputs larger than L2 (database 390 MB vs 129 MB L2)"}
+
+
+# ---- reference arm: the oracle on the host cores ---------------------------------
+def run_reference(args, dist: Dist):
+    if dist.rank != 0:
+        return
+    from oracle import oracle
+    import ngia
+
+    db, cfg = make_db(args)
+    p = ngia.params_clamp(cfg["type"], args.similarity, args.word, 0)
+    cores = os.cpu_count() or 1
+    times, cands = [], []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        _, _, st = oracle.cluster(db.words, db.rec_off, cfg["type"], p.similarity, p.word_length, p.precise,
+                                  threads=0, max_iters=1)
+        dt = time.perf_counter() - t0
+        if k >= args.warmup:
+            times.append(dt)
+            cands.append(st["candidates"])
+    T = sum(times)
+    v = sum(cands) / T
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u32", "impl": "reference",
+           "data": "synthetic (seeded generator with the configuration's shapes)",
+           "config": {**workload_desc(args, cfg), "iters_per_step": 1},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                            "sample": "first greedy iteration (representative vs all 1M sequences) per step"},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ---- our arm ------------------------------------------------------------------------
+def run_ours(args, dist: Dist):
+    import ngia
+
+    ngia.set_device(dist.local)
+    db, cfg = make_db(args)
+    p = ngia.params_clamp(cfg["type"], args.similarity, args.word, 0)
+    mode = ngia.MODE_GRAPH if args.mode == "graph" else ngia.MODE_PLAIN
+    S = args.iters_per_step
+    launches_per_iter = 3 + ngia_classes(cfg["type"])
+    int_gops = ngia.measure_int_peak() if dist.rank == 0 else 0.0
+
+    ctx = ngia.Context(db)
+    ctx.begin(p, mode)
+    for _ in range(args.warmup):
+        ctx.step(S)
+    dist.barrier()
+    st0 = ctx.stats()
+    clocks = Clocks(dist.local)
+    clocks.start()
+    t_wall = time.perf_counter()
+    dev_ms = 0.0
+    for _ in range(args.steps):
+        ctx.step(S)
+        dev_ms += ctx.step_ms()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    st1 = ctx.stats()
+    dist.barrier()
+    cands = st1["candidates"] - st0["candidates"]
+    cells = st1["band_cells"] - st0["band_cells"]
+    T = dist.reduce(dev_ms / 1e3, "max")
+    total_cands = dist.reduce(float(cands), "sum")
+    total_cells = dist.reduce(float(cells), "sum")
+
+    # stage timings (plain driver, CUDA events around the filter and alignment
+    # launches on their stream) for the rooflines
+    ctx.begin(p, ngia.MODE_PLAIN)
+    ctx.step(2)
+    a = ctx.stats()
+    ctx.set_profiling(True)
+    ctx.step(max(4, S // 4))
+    b = ctx.stats()
+    ctx.set_profiling(False)
+    ms_align, ms_filter = b["ms_align"], b["ms_filter"]
+    prof_iters = b["iterations"] - a["iterations"]
+    done_gcell = (b["done_cells"] - a["done_cells"]) / (ms_align * 1e-3) / 1e9
+    band_gcell = (b["band_cells"] - a["band_cells"]) / (ms_align * 1e-3) / 1e9
+    filt_gbs = (b["filter_bytes"] - a["filter_bytes"]) / (ms_filter * 1e-3) / 1e9
+    ctx.close()
+
+    out = None
+    if dist.rank == 0:
+        peak_gcell = int_gops * 32.0 / 4.0  # 4 INT32 operations per 32-cell word step (DNA)
+        peaks = measured_peaks()
+        e2e = None
+        if not args.skip_e2e:
+            e2e = run_e2e(args, db, p, S)
+        cpu = None
+        if not args.skip_cpu and dist.world == 1:
+            cpu = run_cpu_baseline(args, db, p, cfg)
+        out = {"metric": METRIC, "value": total_cands / T, "unit": UNIT, "n_gpus": dist.world,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+               "data": "synthetic (seeded generator with the configuration's shapes)",
+               "config": workload_desc(args, cfg),
+               "gcups": total_cells / T / 1e9,
+               "gcups_note": "reference band cells (func.cu loop bounds) of the pairs aligned, per second",
+               "wall_s_timed": t_wall,
+               "roofline": {"bound": "int32", "kernel": "k_align_* (banded bit-parallel LCS)",
+                            "achieved": done_gcell, "peak": peak_gcell, "unit": "Gcell/s",
+                            "frac": done_gcell / peak_gcell if peak_gcell else None, "traffic": None,
+                            "peak_source": f"of measured INT32 issue rate {int_gops:.0f} Gop/s (probe) x 32 cells"
+                                           f" / 4 ops", "reference_cells_rate": band_gcell,
+                            "profiled_iterations": prof_iters, "ms_align_per_iter": ms_align / prof_iters},
+               "filter_roofline": {"bound": "hbm", "kernel": "k_prep + k_filter", "achieved": filt_gbs,
+                                   "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                   "frac": filt_gbs / peaks["hbm_gbs"], "traffic": None,
+                                   "peak_source": peaks["source"],
+                                   "ms_filter_per_iter": ms_filter / prof_iters},
+               "gpu_launches": launches_per_iter * S * args.steps,
+               "clocks": clk, "cpu_baseline": cpu, "e2e": e2e}
+    db.close()
+    if out is not None:
+        print(json.dumps(out), flush=True)
+
+
+def ngia_classes(db_type: int) -> int:
+    return 6 if db_type == 0 else 4
+
+
+def run_e2e(args, db, p, S):
+    """Through the C ABI with host buffers: open (H2D) + S iterations + results (D2H) + close."""
+    import ngia
+
+    ngia.pin_host(db.words)
+    ngia.pin_host(db.rec_off)
+    try:
+        times, cands = [], []
+        for k in range(1 + args.e2e_steps):
+            t0 = time.perf_counter()
+            ctx = ngia.Context(db)
+            ctx.begin(p, ngia.MODE_GRAPH)
+            ctx.step(S)
+            cl, ident, st = ctx.end()
+            ctx.close()
+            dt = time.perf_counter() - t0
+            if k:
+                times.append(dt)
+                cands.append(st["candidates"])
+    finally:
+        ngia.unpin_host(db.words)
+        ngia.unpin_host(db.rec_off)
+    T = sum(times)
+    return {"value": sum(cands) / T, "unit": UNIT, "h2d_bytes_per_step": int(db.words.nbytes + db.rec_off.nbytes),
+            "d2h_bytes_per_step": int(8 * db.n), "steps": len(times),
+            "per_step": f"ngia_open (database from pinned host memory) + {S} greedy iterations + "
+                        f"ngia_cluster_end (assignment and scores to host) + ngia_close"}
+
+
+def run_cpu_baseline(args, db, p, cfg):
+    from oracle import oracle
+
+    t0 = time.perf_counter()
+    _, _, st1 = oracle.cluster(db.words, db.rec_off, cfg["type"], p.similarity, p.word_length, p.precise,
+                               threads=0, max_iters=1)
+    t1 = time.perf_counter() - t0
+    n_it = max(1, int(args.cpu_seconds / max(t1, 1e-3)))
+    t0 = time.perf_counter()
+    _, _, st = oracle.cluster(db.words, db.rec_off, cfg["type"], p.similarity, p.word_length, p.precise,
+                              threads=0, max_iters=n_it)
+    t = time.perf_counter() - t0
+    return {"value": st["candidates"] / t, "unit": UNIT, "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"first {n_it} greedy iteration(s) of the same workload ({st['candidates']:,} candidates),"
+                      f" C/OpenMP restatement of the reference on all host threads"}
+
+
+def main():
+    args = parse()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, dist)
+        else:
+            run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    main()

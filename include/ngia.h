@@ -148,6 +148,10 @@ typedef struct ngia_stats {
     int64_t band_cells;    /* reference band cells of the alignment pairs    */
     int64_t filter_bytes;  /* algorithmic filter bytes (headers + planes)    */
     int64_t word_checks;   /* pairs the short-word filter was evaluated on   */
+    int64_t done_cells;    /* in-band cells the alignment kernels computed   */
+                           /* (fewer than band_cells: early rejection)       */
+    double  ms_filter;     /* device time of prep + filter launches and      */
+    double  ms_align;      /* of the alignment launches (profiling, plain)   */
 } ngia_stats;
 
 /* Copies the database to the device (one host-to-device transfer) and
@@ -173,6 +177,18 @@ int ngia_cluster_step(ngia_ctx *ctx, int64_t max_iters, int32_t *done);
 int ngia_cluster_end(ngia_ctx *ctx, int32_t *cluster_out,
                      int32_t *identity_out, ngia_stats *stats);
 
+/* Current statistics of the run started by ngia_cluster_begin, without
+ * copying the assignment arrays. */
+int ngia_cluster_stats(ngia_ctx *ctx, ngia_stats *stats);
+
+/* Device time (CUDA events on the context stream) of the last
+ * ngia_cluster_step call. */
+int ngia_step_device_ms(ngia_ctx *ctx, float *ms);
+
+/* 1 = time every stage launch with CUDA events (plain driver form only; the
+ * totals land in ngia_stats.ms_filter / ms_align). */
+int ngia_set_profiling(ngia_ctx *ctx, int32_t on);
+
 /* Per-pair stage values for (rep, cands[k]) pairs, for unit-level parity:
  * out[4k+0] = composition sum, out[4k+1] = short-word count (-1 when the
  * reference skips it because a net length is < 16), out[4k+2] = banded-LCS
@@ -183,6 +199,19 @@ int ngia_pair_scores(ngia_ctx *ctx, const ngia_params *p, int32_t rep,
 
 /* Number of CUDA devices visible to the process (0 when there is none). */
 int ngia_device_count(int32_t *count);
+
+/* Selects the CUDA device for contexts opened later by the calling thread. */
+int ngia_set_device(int32_t device);
+
+/* Page-locks / releases a caller buffer so host<->device copies of it run at
+ * full link speed (e.g. the database words before ngia_open). */
+int ngia_pin_host(void *ptr, size_t bytes);
+int ngia_unpin_host(void *ptr);
+
+/* Measures the INT32 logic/add issue rate of the current device with an
+ * instruction-mix probe (three LOP3 and one IADD3 per step, the mix of the
+ * alignment inner loop); *gops receives lane-operations per second / 1e9. */
+int ngia_measure_int_peak(double *gops);
 
 /* CUDA stream the context launches on (as an opaque handle, for timing). */
 void *ngia_stream(ngia_ctx *ctx);

@@ -25,11 +25,11 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 
-CU_SOURCES = ["csrc/filter.cu", "csrc/align.cu", "csrc/api.cu"]
+CU_SOURCES = ["csrc/filter.cu", "csrc/align.cu", "csrc/api.cu", "csrc/probe.cu"]
 CPP_SOURCES = ["host/errors.cpp", "host/synth.cpp", "host/dbformat.cpp"]
 TOOLS = {"cluster": "host/cluster_main.cpp", "makeDB": "host/makedb_main.cpp", "ngia_synth": "host/synth_main.cpp"}
 
-CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-fopenmp", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
+CXXFLAGS = ["-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-Wall", "-Wno-unused-function"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 
 
@@ -71,7 +71,7 @@ def build(jobs: int | None = None, verbose: bool = False) -> Path:
     lib = OUT / "libngia.so"
     if _stale(lib, objs):
         _run([NVCC] + ARCH + ["-shared", "-o", str(lib)] + [str(o) for o in objs] +
-             ["-cudart", "static", "-Xcompiler", "-fopenmp", "-lgomp"])
+             ["-cudart", "static", "-Xcompiler", "-pthread"])
     for name, src in TOOLS.items():
         exe = OUT / name
         s = PKG / src

@@ -267,16 +267,19 @@ __device__ __forceinline__ void finish_pair(const DevDB &db, const RunBufs &rb, 
 }
 
 __device__ __forceinline__ void flush_align_stats(RunState *st, unsigned long long pairs,
-                                                  unsigned long long members, unsigned long long cells) {
+                                                  unsigned long long members, unsigned long long cells,
+                                                  unsigned long long done) {
   for (int o = 16; o; o >>= 1) {
     pairs += __shfl_down_sync(kFullMask, pairs, o);
     members += __shfl_down_sync(kFullMask, members, o);
     cells += __shfl_down_sync(kFullMask, cells, o);
+    done += __shfl_down_sync(kFullMask, done, o);
   }
   if ((threadIdx.x & 31) == 0) {
     if (pairs) atomicAdd(&st->st_align_pairs, pairs);
     if (members) atomicAdd(&st->st_members, members);
     if (cells) atomicAdd(&st->st_band_cells, cells);
+    if (done) atomicAdd(&st->st_done_cells, done * 32ull);
   }
 }
 
@@ -298,7 +301,7 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_
   int state = -1, entry = 0, cand = 0;
   int i = 0, nq = 0, B = 0, js = 0, je = -1, net2 = 0, L2 = 0, cutoff = 0, lastcols = 32, frozen = 0;
   const uint32_t *qpl = nullptr;
-  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0;
+  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0, n_done = 0;
 
   for (;;) {
     claim(st, cls, h.qn, lane, state);
@@ -340,6 +343,7 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_
     }
     // ---- one 32-residue query block ---------------------------------------
     const int cols = (i == nq - 1) ? lastcols : 32;
+    n_done += (unsigned long long)(je - js + 1) * cols;
     if (i + 1 < nq) {
 #pragma unroll
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
@@ -423,7 +427,7 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_
 #pragma unroll
     for (int p = 0; p < P; p++) cur[p] = nxt[p];
   }
-  flush_align_stats(st, n_pairs, n_members, n_cells);
+  flush_align_stats(st, n_pairs, n_members, n_cells, n_done);
 }
 
 
@@ -479,7 +483,7 @@ __global__ void __launch_bounds__(kAlignThreads, P == 2 ? 3 : 2)
   bool active = false;
   const uint32_t *qpl = nullptr;
   uint32_t cur[P], nxt[P];
-  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0;
+  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0, n_done = 0;
   for (;;) {
     claim(st, cls, h.qn, lane, state);
     if (__all_sync(kFullMask, state == -2)) break;
@@ -514,6 +518,7 @@ __global__ void __launch_bounds__(kAlignThreads, P == 2 ? 3 : 2)
       active = true;
     }
     const int cols = (i == nq - 1) ? lastcols : 32;
+    n_done += (unsigned long long)(je - js + 1) * cols;
     if (i + 1 < nq) {
 #pragma unroll
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
@@ -591,7 +596,7 @@ __global__ void __launch_bounds__(kAlignThreads, P == 2 ? 3 : 2)
 #pragma unroll
     for (int p = 0; p < P; p++) cur[p] = nxt[p];
   }
-  flush_align_stats(st, n_pairs, n_members, n_cells);
+  flush_align_stats(st, n_pairs, n_members, n_cells, n_done);
 }
 
 template <int P>
@@ -618,7 +623,7 @@ __global__ void __launch_bounds__(kAlignThreads) k_align_generic(DevDB db, RunBu
   int state = -1, entry = 0, cand = 0, i = 0, nq = 0, B = 0, net2 = 0, L2 = 0, cutoff = 0, zc = 0;
   bool busy = false;
   const uint32_t *qpl = nullptr;
-  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0;
+  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0, n_done = 0;
   for (;;) {
     claim(st, cls, h.qn, lane, state);
     if (__all_sync(kFullMask, state == -2)) break;
@@ -648,6 +653,7 @@ __global__ void __launch_bounds__(kAlignThreads) k_align_generic(DevDB db, RunBu
 #pragma unroll
       for (int p = 0; p < P; p++) col[p] = qpl[i * P + p];
       const int jstart = max(i - B, 0), jend = min(i + B, nb1 - 1);
+      if (jend >= jstart) n_done += (unsigned long long)(jend - jstart + 1) * cols;
       uint32_t cw = 0;
       for (int j = jstart; j <= jend; j++) {
         uint32_t R[P];
@@ -681,7 +687,7 @@ __global__ void __launch_bounds__(kAlignThreads) k_align_generic(DevDB db, RunBu
       state = -1;
     }
   }
-  flush_align_stats(st, n_pairs, n_members, n_cells);
+  flush_align_stats(st, n_pairs, n_members, n_cells, n_done);
 }
 
 // ---- dispatch ---------------------------------------------------------------------

@@ -46,8 +46,11 @@ int pull_state(ngia_ctx *c) {
 // One greedy iteration: prepare the representative, filter the unclustered
 // set into class queues, align every class, pick the next representative.
 int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond) {
+  const bool prof = c->profiling && !graph;
+  if (prof) CK(cudaEventRecord(c->ev_p0, c->stream));
   CK(ngia::launch_prep(c, -1));
   CK(ngia::launch_filter(c));
+  if (prof) CK(cudaEventRecord(c->ev_p1, c->stream));
   const int nc = ngia::num_classes(c->db.type);
   if (graph) {
     // classes run as parallel branches of the body graph
@@ -61,8 +64,31 @@ int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond) 
   } else {
     for (int k = 0; k < nc; k++) CK(ngia::launch_align(c, k, c->stream, 0));
   }
+  if (prof) CK(cudaEventRecord(c->ev_p2, c->stream));
   CK(ngia::launch_next(c, (unsigned long long)cond, graph ? 1 : 0));
   return NGIA_OK;
+}
+
+// Adds the stage times of the iteration just synchronised (profiling).
+void account_stages(ngia_ctx *c) {
+  float a = 0.f, b = 0.f;
+  if (cudaEventElapsedTime(&a, c->ev_p0, c->ev_p1) == cudaSuccess) c->ms_filter += a;
+  if (cudaEventElapsedTime(&b, c->ev_p1, c->ev_p2) == cudaSuccess) c->ms_align += b;
+}
+
+void fill_stats(const ngia_ctx *c, ngia_stats *stats) {
+  const ngia::RunState &s = *c->h_state;
+  stats->iterations = s.iter;
+  stats->candidates = (int64_t)s.st_candidates;
+  stats->base_pass = (int64_t)s.st_base_pass;
+  stats->align_pairs = (int64_t)s.st_align_pairs;
+  stats->members = (int64_t)s.st_members;
+  stats->band_cells = (int64_t)s.st_band_cells;
+  stats->filter_bytes = (int64_t)s.st_filter_bytes;
+  stats->word_checks = (int64_t)s.st_word_checks;
+  stats->done_cells = (int64_t)s.st_done_cells;
+  stats->ms_filter = c->ms_filter;
+  stats->ms_align = c->ms_align;
 }
 
 void destroy_graph(ngia_ctx *c) {
@@ -140,7 +166,10 @@ extern "C" int ngia_open(const ngia_db_view *v, ngia_ctx **out) {
         cudaEventCreateWithFlags(&c->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
       return bail(fail(NGIA_E_CUDA, "cannot create side streams"));
   }
-  if (cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess)
+  if (cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&c->ev_step0) != cudaSuccess || cudaEventCreate(&c->ev_step1) != cudaSuccess ||
+      cudaEventCreate(&c->ev_p0) != cudaSuccess || cudaEventCreate(&c->ev_p1) != cudaSuccess ||
+      cudaEventCreate(&c->ev_p2) != cudaSuccess)
     return bail(fail(NGIA_E_CUDA, "cannot create event"));
   const int64_t n = v->n;
   const int type = v->type;
@@ -239,6 +268,8 @@ extern "C" int ngia_close(ngia_ctx *c) {
     if (c->join_ev[k]) cudaEventDestroy(c->join_ev[k]);
   }
   if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  for (cudaEvent_t ev : {c->ev_step0, c->ev_step1, c->ev_p0, c->ev_p1, c->ev_p2})
+    if (ev) cudaEventDestroy(ev);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return NGIA_OK;
@@ -267,6 +298,8 @@ extern "C" int ngia_cluster_begin(ngia_ctx *c, const ngia_params *p, int32_t mod
   if (const char *wo = getenv("NGIA_WORD_ORDER")) c->prm.word_order = atoi(wo);
   if (c->db.has_short && !c->prm.precise) c->prm.word_order = 1;  // exact path is word first
   c->mode = mode;
+  c->ms_filter = c->ms_align = 0.0;
+  c->last_step_ms = 0.f;
   CK(ngia::launch_init_run(c));
   rc = pull_state(c);
   if (rc) return rc;
@@ -289,19 +322,66 @@ extern "C" int ngia_cluster_step(ngia_ctx *c, int64_t max_iters, int32_t *done) 
     c->h_state->iter_limit = max_iters > 0 ? c->h_state->iter + max_iters : LLONG_MAX;
     CK(cudaMemcpyAsync(&c->rb.st->iter_limit, &c->h_state->iter_limit, sizeof(int64_t), cudaMemcpyHostToDevice,
                        c->stream));
+    CK(cudaEventRecord(c->ev_step0, c->stream));
     CK(cudaGraphLaunch(c->graph_exec, c->stream));
+    CK(cudaEventRecord(c->ev_step1, c->stream));
     int rc = pull_state(c);
     if (rc) return rc;
   } else {
+    CK(cudaEventRecord(c->ev_step0, c->stream));
     for (int64_t it = 0; max_iters <= 0 || it < max_iters; it++) {
       int rc = enqueue_iteration(c, false, 0);
       if (rc) return rc;
       rc = pull_state(c);  // the per-representative host round trip of the plain form
       if (rc) return rc;
+      if (c->profiling) account_stages(c);
       if (c->h_state->done) break;
     }
+    CK(cudaEventRecord(c->ev_step1, c->stream));
+    CK(cudaEventSynchronize(c->ev_step1));
   }
+  CK(cudaEventElapsedTime(&c->last_step_ms, c->ev_step0, c->ev_step1));
   if (done) *done = c->h_state->done;
+  return NGIA_OK;
+}
+
+extern "C" int ngia_step_device_ms(ngia_ctx *c, float *ms) {
+  if (!c || !ms) return fail(NGIA_E_ARG, "ngia_step_device_ms: null argument");
+  *ms = c->last_step_ms;
+  return NGIA_OK;
+}
+
+extern "C" int ngia_set_profiling(ngia_ctx *c, int32_t on) {
+  if (!c) return fail(NGIA_E_ARG, "ngia_set_profiling: null context");
+  c->profiling = on != 0;
+  return NGIA_OK;
+}
+
+extern "C" int ngia_cluster_stats(ngia_ctx *c, ngia_stats *stats) {
+  if (!c || !stats) return fail(NGIA_E_ARG, "ngia_cluster_stats: null argument");
+  if (!c->begun) return fail(NGIA_E_STATE, "ngia_cluster_stats before ngia_cluster_begin");
+  int rc = pull_state(c);
+  if (rc) return rc;
+  fill_stats(c, stats);
+  return NGIA_OK;
+}
+
+extern "C" int ngia_set_device(int32_t device) {
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) return fail(NGIA_E_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+  return NGIA_OK;
+}
+
+extern "C" int ngia_pin_host(void *ptr, size_t bytes) {
+  if (!ptr || !bytes) return fail(NGIA_E_ARG, "ngia_pin_host: empty buffer");
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) return fail(NGIA_E_CUDA, "cudaHostRegister: %s", cudaGetErrorString(e));
+  return NGIA_OK;
+}
+
+extern "C" int ngia_unpin_host(void *ptr) {
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) return fail(NGIA_E_CUDA, "cudaHostUnregister: %s", cudaGetErrorString(e));
   return NGIA_OK;
 }
 
@@ -313,17 +393,7 @@ extern "C" int ngia_cluster_end(ngia_ctx *c, int32_t *cluster_out, int32_t *iden
   if (identity_out) CK(cudaMemcpyAsync(identity_out, c->rb.ident, 4 * n, cudaMemcpyDeviceToHost, c->stream));
   int rc = pull_state(c);
   if (rc) return rc;
-  if (stats) {
-    const ngia::RunState &s = *c->h_state;
-    stats->iterations = s.iter;
-    stats->candidates = (int64_t)s.st_candidates;
-    stats->base_pass = (int64_t)s.st_base_pass;
-    stats->align_pairs = (int64_t)s.st_align_pairs;
-    stats->members = (int64_t)s.st_members;
-    stats->band_cells = (int64_t)s.st_band_cells;
-    stats->filter_bytes = (int64_t)s.st_filter_bytes;
-    stats->word_checks = (int64_t)s.st_word_checks;
-  }
+  if (stats) fill_stats(c, stats);
   return NGIA_OK;
 }
 

@@ -71,6 +71,7 @@ struct RunState {
   // statistics (device-accumulated)
   unsigned long long st_candidates, st_base_pass, st_align_pairs, st_members;
   unsigned long long st_band_cells, st_filter_bytes, st_word_checks, st_word_pass;
+  unsigned long long st_done_cells;  // in-band cells actually computed
 };
 
 // Run parameters (constant during one clustering).

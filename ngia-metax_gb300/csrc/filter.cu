@@ -90,6 +90,7 @@ __global__ void k_init_run(DevDB db, RunBufs rb, RunParams prm) {
     st->rep_nb = st->rep_len = st->rep_net = 0;
     st->st_candidates = st->st_base_pass = st->st_align_pairs = st->st_members = 0;
     st->st_band_cells = st->st_filter_bytes = st->st_word_checks = st->st_word_pass = 0;
+    st->st_done_cells = 0;
   }
 }
 

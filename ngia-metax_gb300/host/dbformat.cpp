@@ -230,11 +230,10 @@ extern "C" int ngia_db_pack(int32_t type, const char *seq, const int64_t *seq_of
   db->view.longest = db->read_len[0];
   db->view.shortest = db->read_len[N - 1];
   uint32_t *w = const_cast<uint32_t *>(db->view.words);
-#pragma omp parallel for schedule(dynamic, 256)
-  for (int64_t k = 0; k < N; k++) {
+  ngia::parallel_for(N, 256, [&](int64_t k) {
     int64_t i = keep[(size_t)k];
     pack_record(type, seq + seq_off[i], seq_off[i + 1] - seq_off[i], w + db->view.rec_off[k]);
-  }
+  });
   *out = db;
   return NGIA_OK;
 }
@@ -281,15 +280,12 @@ extern "C" int ngia_makedb(const char *fasta_path, const char *outdir, int32_t t
   }
   layout(db, type);
   uint32_t *w = const_cast<uint32_t *>(db->view.words);
-#pragma omp parallel
-  {
-    std::string s;
-#pragma omp for schedule(dynamic, 256)
-    for (int64_t i = 0; i < N; i++) {
-      record_sequence(text, recs[(size_t)i], s);
-      pack_record(type, s.data(), (int64_t)s.size(), w + db->view.rec_off[i]);
-    }
-  }
+  std::vector<std::string> scratch((size_t)ngia::hardware_threads());
+  ngia::parallel_for(N, 256, [&](int64_t i, int t) {
+    std::string &s = scratch[(size_t)t];
+    record_sequence(text, recs[(size_t)i], s);
+    pack_record(type, s.data(), (int64_t)s.size(), w + db->view.rec_off[i]);
+  });
   std::string bin = dir + "/data.bin";
   FILE *f = std::fopen(bin.c_str(), "wb");
   if (!f) {

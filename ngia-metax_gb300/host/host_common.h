@@ -1,10 +1,15 @@
 // host_common.h — shared helpers of the host half of libngia (error state,
 // makeDB record geometry).  Internal header: not part of the C ABI.
 #pragma once
+#include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <thread>
+#include <type_traits>
+#include <vector>
 
 #include "../../include/ngia.h"
 
@@ -26,5 +31,34 @@ inline int64_t record_words(int type, int64_t len) {
 
 // Maximum raw length makeDB keeps (makeDB.cpp:92).
 constexpr int kMaxLen = 65536;
+
+// Runs body(i) for i in [0, n) on all hardware threads, handing out chunks of
+// `grain` indices from an atomic counter.  body(i, thread) when it takes two
+// arguments (per-thread scratch).
+template <class F>
+void parallel_for(int64_t n, int64_t grain, F body) {
+  if (n <= 0) return;
+  const int64_t nchunks = (n + grain - 1) / grain;
+  int nt = (int)std::min<int64_t>(std::max(1u, std::thread::hardware_concurrency()), nchunks);
+  std::atomic<int64_t> next{0};
+  auto work = [&](int t) {
+    for (;;) {
+      const int64_t c = next.fetch_add(1);
+      if (c >= nchunks) break;
+      const int64_t e = std::min(n, (c + 1) * grain);
+      for (int64_t i = c * grain; i < e; i++) {
+        if constexpr (std::is_invocable_v<F, int64_t, int>)
+          body(i, t);
+        else
+          body(i);
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; t++) th.emplace_back(work, t);
+  work(0);
+  for (auto &x : th) x.join();
+}
+inline int hardware_threads() { return (int)std::max(1u, std::thread::hardware_concurrency()); }
 
 }  // namespace ngia

@@ -207,30 +207,35 @@ extern "C" int ngia_synth_generate(const ngia_synth_params *pp, char **seq,
   std::vector<std::string> anc((size_t)p.n_ancestors), novel;
   size_t n_novel = p.novel_frac > 0.0 ? (size_t)p.n_ancestors : 0;
   novel.resize(n_novel);
-#pragma omp parallel for schedule(dynamic, 64)
-  for (int64_t a = 0; a < (int64_t)anc.size() + (int64_t)n_novel; a++) {
+  ngia::parallel_for((int64_t)anc.size() + (int64_t)n_novel, 64, [&](int64_t a) {
     if (a < (int64_t)anc.size())
       anc[(size_t)a] = make_ancestor(p, ab, kTagAncestor, a);
     else
       novel[(size_t)(a - (int64_t)anc.size())] =
           make_ancestor(p, ab, kTagNovel, a - (int64_t)anc.size());
-  }
+  });
 
   const int64_t N = p.n_seqs;
   const int64_t chunk = 2048;
   const int64_t nchunks = (N + chunk - 1) / chunk;
   std::vector<std::string> parts((size_t)nchunks);
   std::vector<std::vector<int64_t>> lens((size_t)nchunks);
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int64_t c = 0; c < nchunks; c++) {
-    std::string tmp;
+  // One allocation per chunk (sized for the longest possible descendants) and
+  // one scratch string per thread.
+  const size_t max_desc = (size_t)p.len_max + (size_t)p.len_max / 4 + 64;
+  std::vector<std::string> scratch((size_t)ngia::hardware_threads());
+  ngia::parallel_for(nchunks, 1, [&](int64_t c, int t) {
+    std::string &tmp = scratch[(size_t)t];
     std::string &dst = parts[(size_t)c];
-    for (int64_t i = c * chunk; i < std::min(N, (c + 1) * chunk); i++) {
+    const int64_t cnt = std::min(N, (c + 1) * chunk) - c * chunk;
+    dst.reserve((size_t)cnt * max_desc);
+    lens[(size_t)c].reserve((size_t)cnt);
+    for (int64_t i = c * chunk; i < c * chunk + cnt; i++) {
       make_descendant(p, ab, anc, novel, i, tmp);
       dst += tmp;
       lens[(size_t)c].push_back((int64_t)tmp.size());
     }
-  }
+  });
   int64_t total = 0;
   for (auto &s : parts) total += (int64_t)s.size();
   char *buf = (char *)std::malloc((size_t)total + 1);

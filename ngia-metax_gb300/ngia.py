@@ -48,10 +48,12 @@ class SynthParams(C.Structure):
 
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("iterations", "candidates", "base_pass", "align_pairs", "members",
-                                         "band_cells", "filter_bytes", "word_checks")]
+                                         "band_cells", "filter_bytes", "word_checks", "done_cells")] + \
+        [("ms_filter", C.c_double), ("ms_align", C.c_double)]
 
     def as_dict(self) -> dict:
-        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+        return {n: (float(getattr(self, n)) if n.startswith("ms_") else int(getattr(self, n)))
+                for n, _ in self._fields_}
 
 
 _lib = None
@@ -86,6 +88,13 @@ def lib() -> C.CDLL:
         "ngia_pair_scores": (C.c_int, [VP, P(Params), I32, P(I32), I32, P(I32)]),
         "ngia_stream": (VP, [VP]),
         "ngia_device_count": (C.c_int, [P(I32)]),
+        "ngia_set_device": (C.c_int, [I32]),
+        "ngia_pin_host": (C.c_int, [VP, C.c_size_t]),
+        "ngia_unpin_host": (C.c_int, [VP]),
+        "ngia_measure_int_peak": (C.c_int, [P(C.c_double)]),
+        "ngia_cluster_stats": (C.c_int, [VP, P(Stats)]),
+        "ngia_step_device_ms": (C.c_int, [VP, P(C.c_float)]),
+        "ngia_set_profiling": (C.c_int, [VP, I32]),
         "ngia_close": (C.c_int, [VP]),
     }
     for name, (res, args) in sig.items():
@@ -117,6 +126,25 @@ def device_count() -> int:
     return n.value
 
 
+def set_device(dev: int) -> None:
+    _check(lib().ngia_set_device(dev))
+
+
+def measure_int_peak() -> float:
+    """INT32 lane-operations per second / 1e9 of the current device (probe)."""
+    g = C.c_double()
+    _check(lib().ngia_measure_int_peak(C.byref(g)))
+    return g.value
+
+
+def pin_host(arr: np.ndarray) -> None:
+    _check(lib().ngia_pin_host(arr.ctypes.data, arr.nbytes))
+
+
+def unpin_host(arr: np.ndarray) -> None:
+    _check(lib().ngia_unpin_host(arr.ctypes.data))
+
+
 def params_clamp(db_type: int, similarity: float, word_length: int, precise: int = 0) -> Params:
     p = Params(similarity, word_length, precise)
     _check(lib().ngia_params_clamp(db_type, C.byref(p)))
@@ -137,10 +165,50 @@ CONFIGS = {
 }
 
 
+class Seqs:
+    """Generated residues, owned by the library (no Python-side copy).
+
+    ``seq`` is a zero-copy uint8 view, ``off`` the int64 offsets[n+1];
+    ``bytes(i)`` returns sequence i."""
+
+    def __init__(self, ptr: C.c_void_p, off: np.ndarray):
+        self._ptr = ptr
+        self.off = off
+        size = int(off[-1])
+        self.seq = (np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_uint8)), shape=(size,)) if size
+                    else np.zeros(0, np.uint8))
+
+    @property
+    def n(self) -> int:
+        return len(self.off) - 1
+
+    def bytes(self, i: int) -> bytes:
+        return self.seq[self.off[i]:self.off[i + 1]].tobytes()
+
+    def all_bytes(self) -> list[bytes]:
+        return [self.bytes(i) for i in range(self.n)]
+
+    def close(self) -> None:
+        if self._ptr:
+            lib().ngia_free(self._ptr)
+            self._ptr = None
+            self.seq = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __iter__(self):  # (seq, off) unpacking
+        yield self
+        yield self.off
+
+
 def synth(type: int = 0, n_seqs: int = 1000, n_ancestors: int = 20, len_dist: int = 0, len_a: float = 1450.0,
           len_b: float = 80.0, len_min: int = 1200, len_max: int = 1700, subst_max: float = 0.2,
-          indel_frac: float = 0.05, indel_max: int = 3, novel_frac: float = 0.0, seed: int = 1):
-    """Generates sequences; returns (bytes of all residues, int64 offsets[n+1])."""
+          indel_frac: float = 0.05, indel_max: int = 3, novel_frac: float = 0.0, seed: int = 1) -> Seqs:
+    """Generates sequences (library-owned buffer); unpacks as (seqs, offsets)."""
     p = SynthParams(type, len_dist, n_seqs, n_ancestors, len_min, len_max, len_a, len_b, subst_max, indel_frac,
                     indel_max, novel_frac, seed)
     seq = C.c_void_p()
@@ -149,16 +217,26 @@ def synth(type: int = 0, n_seqs: int = 1000, n_ancestors: int = 20, len_dist: in
     _check(lib().ngia_synth_generate(C.byref(p), C.byref(seq), C.byref(off), C.byref(n)))
     try:
         offs = np.ctypeslib.as_array(off, shape=(n.value + 1,)).copy()
-        data = C.string_at(seq, int(offs[-1]))
     finally:
-        lib().ngia_free(seq)
         lib().ngia_free(C.cast(off, C.c_void_p))
-    return data, offs
+    return Seqs(seq, offs)
 
 
-def write_fasta(path: str, seq: bytes, off: np.ndarray, width: int = 80) -> None:
+def _seq_ptr(seq):
+    """Pointer to residue bytes given bytes, a uint8 array or a Seqs."""
+    if isinstance(seq, Seqs):
+        return C.cast(seq._ptr, C.c_char_p), seq
+    if isinstance(seq, np.ndarray):
+        a = np.ascontiguousarray(seq, dtype=np.uint8)
+        return a.ctypes.data_as(C.c_char_p), a
+    return seq, seq
+
+
+def write_fasta(path: str, seq, off: np.ndarray, width: int = 80) -> None:
     off = np.ascontiguousarray(off, dtype=np.int64)
-    _check(lib().ngia_write_fasta(str(path).encode(), seq, _i64p(off), len(off) - 1, width))
+    ptr, keep = _seq_ptr(seq)
+    _check(lib().ngia_write_fasta(str(path).encode(), ptr, _i64p(off), len(off) - 1, width))
+    del keep
 
 
 class DB:
@@ -187,10 +265,12 @@ class DB:
         return cls(p)
 
     @classmethod
-    def pack(cls, db_type: int, seq: bytes, off: np.ndarray) -> "DB":
+    def pack(cls, db_type: int, seq, off: np.ndarray) -> "DB":
         off = np.ascontiguousarray(off, dtype=np.int64)
         p = C.POINTER(DBHost)()
-        _check(lib().ngia_db_pack(db_type, seq, _i64p(off), len(off) - 1, None, C.byref(p)))
+        ptr, keep = _seq_ptr(seq)
+        _check(lib().ngia_db_pack(db_type, ptr, _i64p(off), len(off) - 1, None, C.byref(p)))
+        del keep
         return cls(p)
 
     def record(self, i: int) -> np.ndarray:
@@ -254,6 +334,19 @@ class Context:
         st = Stats()
         _check(lib().ngia_cluster_end(self._h, _i32p(cl), _i32p(ident), C.byref(st)))
         return cl, ident, st.as_dict()
+
+    def stats(self) -> dict:
+        st = Stats()
+        _check(lib().ngia_cluster_stats(self._h, C.byref(st)))
+        return st.as_dict()
+
+    def step_ms(self) -> float:
+        ms = C.c_float()
+        _check(lib().ngia_step_device_ms(self._h, C.byref(ms)))
+        return ms.value
+
+    def set_profiling(self, on: bool) -> None:
+        _check(lib().ngia_set_profiling(self._h, 1 if on else 0))
 
     def pair_scores(self, params: Params, rep: int, cands) -> np.ndarray:
         c = np.ascontiguousarray(cands, dtype=np.int32)

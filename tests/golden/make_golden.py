@@ -87,7 +87,7 @@ def make_fasta() -> None:
     manifest = {}
     for name, typ, gen, kind, params in FIXTURES:
         seq, off = ngia.synth(**gen)
-        seqs = [seq[off[i]:off[i + 1]] for i in range(len(off) - 1)]
+        seqs = seq.all_bytes()
         if kind == "noisy":
             seqs = _noisy(seqs, gen["seed"])
         fa = HERE / f"{name}.fasta"

@@ -13,8 +13,10 @@ def seqs_to_db(db_type: int, seqs: list[bytes]) -> "ngia.DB":
     return ngia.DB.pack(db_type, b"".join(seqs), off)
 
 
-def split(seq: bytes, off: np.ndarray) -> list[bytes]:
-    return [seq[off[i]:off[i + 1]] for i in range(len(off) - 1)]
+def split(seq, off: np.ndarray) -> list[bytes]:
+    if isinstance(seq, ngia.Seqs):
+        return seq.all_bytes()
+    return [bytes(seq[off[i]:off[i + 1]]) for i in range(len(off) - 1)]
 
 
 def family_db(db_type: int = 0, n: int = 400, anc: int = 8, seed: int = 1, **kw) -> "ngia.DB":

@@ -291,10 +291,10 @@ def test_oracle_stage_counts_are_consistent():
 def test_synth_is_deterministic_and_clipped():
     a = ngia.synth(n_seqs=300, n_ancestors=7, seed=9)
     b = ngia.synth(n_seqs=300, n_ancestors=7, seed=9)
-    assert a[0] == b[0] and np.array_equal(a[1], b[1])
+    assert np.array_equal(a.seq, b.seq) and np.array_equal(a.off, b.off)
     c = ngia.synth(**{**ngia.CONFIGS["protein_200k"], "n_seqs": 500, "seed": 3})
-    lens = np.diff(c[1])
-    assert lens.min() >= 1 and set(c[0]) <= set(b"ARNDCQEGHILKMFPSTWYV")
+    lens = np.diff(c.off)
+    assert lens.min() >= 1 and set(c.seq.tobytes()) <= set(b"ARNDCQEGHILKMFPSTWYV")
 
 
 SYNTH_MD5 = "d8b9bb5e1a8a3d7ce0d7b2f0b4a1f3c0"
