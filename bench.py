@@ -277,7 +277,11 @@ def run_ours(args, dist: Dist):
                             "frac": done_gcell / peak_gcell if peak_gcell else None, "traffic": None,
                             "peak_source": f"of measured INT32 issue rate {int_gops:.0f} Gop/s (probe) x 32 cells"
                                            f" / 4 ops", "reference_cells_rate": band_gcell,
-                            "profiled_iterations": prof_iters, "ms_align_per_iter": ms_align / prof_iters},
+                            "profiled_iterations": prof_iters, "ms_align_per_iter": ms_align / prof_iters,
+                            "class_ms_per_iter": [round((y - x) / prof_iters, 3) for x, y in
+                                                  zip(a["class_ms"], b["class_ms"])],
+                            "class_pairs_per_iter": [round((y - x) / prof_iters) for x, y in
+                                                     zip(a["class_pairs"], b["class_pairs"])]},
                "filter_roofline": {"bound": "hbm", "kernel": "k_prep + k_filter", "achieved": filt_gbs,
                                    "peak": peaks["hbm_gbs"], "unit": "GB/s",
                                    "frac": filt_gbs / peaks["hbm_gbs"], "traffic": None,
@@ -291,7 +295,7 @@ def run_ours(args, dist: Dist):
 
 
 def ngia_classes(db_type: int) -> int:
-    return 6 if db_type == 0 else 4
+    return 7 if db_type == 0 else 5
 
 
 def run_e2e(args, db, p, S):

@@ -152,6 +152,8 @@ typedef struct ngia_stats {
                            /* (fewer than band_cells: early rejection)       */
     double  ms_filter;     /* device time of prep + filter launches and      */
     double  ms_align;      /* of the alignment launches (profiling, plain)   */
+    int64_t class_pairs[8];   /* pairs queued per alignment work class       */
+    double  class_ms[8];      /* device time per class (profiling, plain)    */
 } ngia_stats;
 
 /* Copies the database to the device (one host-to-device transfer) and

@@ -33,8 +33,10 @@
 // updated segment), so zeros_now + residues_left < cutoff is a rejection.
 // Accepted pairs are always computed to the end (their score is reported).
 #include <climits>
+#include <cstdlib>
 
 #include "ctx.h"
+#include "dp_asm.cuh"
 
 namespace ngia {
 
@@ -45,116 +47,6 @@ constexpr int kAlignThreads = 128;  // threads per CTA of every alignment kernel
 // register-window kernel of P planes and WC slots.
 __host__ __device__ constexpr int win_min_blocks(int P, int WC) {
   return P == 2 ? (WC <= 8 ? 6 : WC <= 16 ? 4 : WC <= 24 ? 3 : 2) : (WC <= 8 ? 4 : 2);
-}
-
-// ---- multi-word addition on the carry flag -------------------------------------
-// t[0..7] = r[0..7] + x[0..7] (+ carry in), least significant word first.
-template <bool FIRST, bool LAST>
-struct Add8;
-
-template <>
-struct Add8<true, true> {
-  static __device__ __forceinline__ void run(const uint32_t *r, const uint32_t *x, uint32_t *t, uint32_t &) {
-    asm("add.cc.u32 %0, %8, %16;\n\t"
-        "addc.cc.u32 %1, %9, %17;\n\t"
-        "addc.cc.u32 %2, %10, %18;\n\t"
-        "addc.cc.u32 %3, %11, %19;\n\t"
-        "addc.cc.u32 %4, %12, %20;\n\t"
-        "addc.cc.u32 %5, %13, %21;\n\t"
-        "addc.cc.u32 %6, %14, %22;\n\t"
-        "addc.u32 %7, %15, %23;"
-        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7])
-        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(x[0]),
-          "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]));
-  }
-};
-template <>
-struct Add8<true, false> {
-  static __device__ __forceinline__ void run(const uint32_t *r, const uint32_t *x, uint32_t *t, uint32_t &c) {
-    asm("add.cc.u32 %0, %9, %17;\n\t"
-        "addc.cc.u32 %1, %10, %18;\n\t"
-        "addc.cc.u32 %2, %11, %19;\n\t"
-        "addc.cc.u32 %3, %12, %20;\n\t"
-        "addc.cc.u32 %4, %13, %21;\n\t"
-        "addc.cc.u32 %5, %14, %22;\n\t"
-        "addc.cc.u32 %6, %15, %23;\n\t"
-        "addc.cc.u32 %7, %16, %24;\n\t"
-        "addc.u32 %8, 0, 0;"
-        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7]),
-          "=r"(c)
-        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(x[0]),
-          "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]));
-  }
-};
-template <>
-struct Add8<false, true> {
-  static __device__ __forceinline__ void run(const uint32_t *r, const uint32_t *x, uint32_t *t, uint32_t &c) {
-    asm("{\n\t.reg .u32 d;\n\t"
-        "add.cc.u32 d, %24, 0xFFFFFFFF;\n\t"
-        "addc.cc.u32 %0, %8, %16;\n\t"
-        "addc.cc.u32 %1, %9, %17;\n\t"
-        "addc.cc.u32 %2, %10, %18;\n\t"
-        "addc.cc.u32 %3, %11, %19;\n\t"
-        "addc.cc.u32 %4, %12, %20;\n\t"
-        "addc.cc.u32 %5, %13, %21;\n\t"
-        "addc.cc.u32 %6, %14, %22;\n\t"
-        "addc.u32 %7, %15, %23;\n\t}"
-        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7])
-        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(x[0]),
-          "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]), "r"(c));
-  }
-};
-template <>
-struct Add8<false, false> {
-  static __device__ __forceinline__ void run(const uint32_t *r, const uint32_t *x, uint32_t *t, uint32_t &c) {
-    asm("{\n\t.reg .u32 d;\n\t"
-        "add.cc.u32 d, %25, 0xFFFFFFFF;\n\t"
-        "addc.cc.u32 %0, %9, %17;\n\t"
-        "addc.cc.u32 %1, %10, %18;\n\t"
-        "addc.cc.u32 %2, %11, %19;\n\t"
-        "addc.cc.u32 %3, %12, %20;\n\t"
-        "addc.cc.u32 %4, %13, %21;\n\t"
-        "addc.cc.u32 %5, %14, %22;\n\t"
-        "addc.cc.u32 %6, %15, %23;\n\t"
-        "addc.cc.u32 %7, %16, %24;\n\t"
-        "addc.u32 %8, 0, 0;\n\t}"
-        : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7]),
-          "=r"(c)
-        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(x[0]),
-          "r"(x[1]), "r"(x[2]), "r"(x[3]), "r"(x[4]), "r"(x[5]), "r"(x[6]), "r"(x[7]), "r"(c));
-  }
-};
-
-// One query residue over the whole register window: x = row & match,
-// row = (row + x (+ carries)) | (row & ~match).
-template <int P, int WC>
-__device__ __forceinline__ void dp_column(uint32_t (&row)[WC], const uint32_t (&pl)[P][WC], const uint32_t (&mk)[P]) {
-  // 8 slots at a time end to end, so only 16 temporaries are live beside the
-  // window; the carry between chunks travels in a register.
-  uint32_t carry = 0;
-#pragma unroll
-  for (int ch = 0; ch < WC / 8; ch++) {
-    uint32_t x[8], t[8];
-#pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int m = 8 * ch + q;
-      uint32_t a = row[m];
-#pragma unroll
-      for (int p = 0; p < P; p++) a &= ~(pl[p][m] ^ mk[p]);
-      x[q] = a;
-    }
-    const uint32_t *rr = row + 8 * ch;
-    if (WC == 8)
-      Add8<true, true>::run(rr, x, t, carry);
-    else if (ch == 0)
-      Add8<true, false>::run(rr, x, t, carry);
-    else if (ch == WC / 8 - 1)
-      Add8<false, true>::run(rr, x, t, carry);
-    else
-      Add8<false, false>::run(rr, x, t, carry);
-#pragma unroll
-    for (int q = 0; q < 8; q++) row[8 * ch + q] = t[q] | (row[8 * ch + q] ^ x[q]);
-  }
 }
 
 struct AlignHdr {
@@ -351,6 +243,7 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_
     uint32_t rv[P];
 #pragma unroll
     for (int p = 0; p < P; p++) rv[p] = __brev(cur[p]);
+    uint32_t cw_unused = 0;
     int k = 0;
     for (; k + 2 <= cols; k += 2) {
       uint32_t mk[P];
@@ -359,19 +252,19 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_
         mk[p] = (uint32_t)((int)rv[p] >> 31);
         rv[p] <<= 1;
       }
-      dp_column<P, WC>(row, pl, mk);
+      dp_tile<P, WC, false, false>(row, pl, mk, cw_unused, cw_unused);
 #pragma unroll
       for (int p = 0; p < P; p++) {
         mk[p] = (uint32_t)((int)rv[p] >> 31);
         rv[p] <<= 1;
       }
-      dp_column<P, WC>(row, pl, mk);
+      dp_tile<P, WC, false, false>(row, pl, mk, cw_unused, cw_unused);
     }
     if (k < cols) {
       uint32_t mk[P];
 #pragma unroll
       for (int p = 0; p < P; p++) mk[p] = (uint32_t)((int)rv[p] >> 31);
-      dp_column<P, WC>(row, pl, mk);
+      dp_tile<P, WC, false, false>(row, pl, mk, cw_unused, cw_unused);
     }
     // ---- slide the band to query block i+1 --------------------------------
     i++;
@@ -431,39 +324,65 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_
 }
 
 
-// One query residue over a TW-slot register tile whose carry enters from and
-// leaves to a register (the tiles of one window are chained through it).
-template <int P, int TW>
-__device__ __forceinline__ void dp_tile_column(uint32_t (&row)[TW], const uint32_t (&pl)[P][TW],
-                                               const uint32_t (&mk)[P], uint32_t &carry) {
+// One register tile of TW window slots starting at rep block `base` for all
+// `cols` residues of the current query block: rows come from and return to
+// the shared-memory ring, planes from the staged representative.  The 32
+// column carries enter in `cw` (column 0 at bit 31; zero for the lowest
+// tile) and leave in `ncw` (ignored after the highest tile).  Slots past `je`
+// are padding: computed, never stored.  Returns the change of the tile's
+// zero count (all bits).
+template <int P, int TW, int RING>
+__device__ __forceinline__ int tiled_tile(uint32_t *ring, const uint32_t *s_pl, int base, int je, int cols,
+                                          const uint32_t (&cur)[P], uint32_t &cw, uint32_t &ncw) {
+  constexpr int RS = kAlignThreads;
+  uint32_t row[TW], pl[P][TW];
+  int zold = 0;
 #pragma unroll
-  for (int ch = 0; ch < TW / 8; ch++) {
-    uint32_t x[8], t[8];
+  for (int m = 0; m < TW; m++) {
+    const int j = base + m;
+    const bool in = j <= je;
+    row[m] = in ? ring[(j & (RING - 1)) * RS] : 0u;
+    zold += in ? __popc(~row[m]) : 0;
 #pragma unroll
-    for (int q = 0; q < 8; q++) {
-      const int m = 8 * ch + q;
-      uint32_t a = row[m];
-#pragma unroll
-      for (int p = 0; p < P; p++) a &= ~(pl[p][m] ^ mk[p]);
-      x[q] = a;
-    }
-    Add8<false, false>::run(row + 8 * ch, x, t, carry);
-#pragma unroll
-    for (int q = 0; q < 8; q++) row[8 * ch + q] = t[q] | (row[8 * ch + q] ^ x[q]);
+    for (int p = 0; p < P; p++) pl[p][m] = in ? s_pl[j * P + p] : 0u;
   }
+  uint32_t rv[P];
+#pragma unroll
+  for (int p = 0; p < P; p++) rv[p] = __brev(cur[p]);
+#pragma unroll 2
+  for (int k = 0; k < cols; k++) {
+    uint32_t mk[P];
+#pragma unroll
+    for (int p = 0; p < P; p++) {
+      mk[p] = (uint32_t)((int)rv[p] >> 31);
+      rv[p] <<= 1;
+    }
+    dp_tile<P, TW, true, true>(row, pl, mk, cw, ncw);
+  }
+  int znew = 0;
+#pragma unroll
+  for (int m = 0; m < TW; m++) {
+    const int j = base + m;
+    if (j <= je) {
+      ring[(j & (RING - 1)) * RS] = row[m];
+      znew += __popc(~row[m]);
+    }
+  }
+  return znew - zold;
 }
 
-// Tiled window: windows of up to kRingBlocks rep blocks.  Each lane keeps its
+// Tiled window: windows of up to RING rep blocks.  Each lane keeps its
 // pair's band rows in a shared-memory ring indexed by absolute rep block
-// (ring[(j mod kRingBlocks) * threads + tid], so the 32 lanes of a warp hit 32
-// distinct banks whatever their j), and runs each query block tile by tile
-// over 16-slot register tiles in ascending rep-block order, all 32 residues
-// per tile, passing the 32 column carries between tiles in one word.  This is
-// the reference's (i, j, k) loop order at tile granularity.
-template <int P>
-__global__ void __launch_bounds__(kAlignThreads, P == 2 ? 3 : 2)
+// (ring[(j mod RING) * threads + tid], so the 32 lanes of a warp hit 32
+// distinct banks whatever their j), and runs each query block tile by tile in
+// ascending rep-block order, all residues of the block per tile — the
+// reference's (i, j, k) loop order at tile granularity.  Full tiles are 16
+// slots; the remainder runs as a 4, 8, 12 or 16-slot tile (at most 3 padding
+// slots); the column carries pass between tiles in one word (one instruction
+// to pop a carry, one to push it).
+template <int P, int RING>
+__global__ void __launch_bounds__(kAlignThreads, P == 2 ? (RING <= 64 ? 4 : 3) : 2)
     k_align_tiled(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode) {
-  constexpr int TW = 16;
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
   AlignHdr h;
@@ -487,8 +406,10 @@ __global__ void __launch_bounds__(kAlignThreads, P == 2 ? 3 : 2)
   for (;;) {
     claim(st, cls, h.qn, lane, state);
     if (__all_sync(kFullMask, state == -2)) break;
-    if (state < 0) continue;
-    if (!active) {
+    // No lane leaves the loop body early: the warp-wide reductions below are
+    // executed by all 32 lanes (lanes without a pair contribute neutral values).
+    bool busy = state >= 0;
+    if (busy && !active) {
       entry = rb.queue[cls][state];
       cand = score_mode ? rb.score_cands[entry] : entry;
       L2 = __ldg(db.len + cand);
@@ -510,79 +431,67 @@ __global__ void __launch_bounds__(kAlignThreads, P == 2 ? 3 : 2)
       if (B < 0 || je < 0 || nq == 0) {
         finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, 0, cutoff, L2, net2, qpl, s_list, n_members);
         state = -1;
-        continue;
-      }
-      for (int j = 0; j <= je; j++) ring[(j & (kRingBlocks - 1)) * RS] = 0xFFFFFFFFu;
+        busy = false;
+      } else {
+        for (int j = 0; j <= je; j++) ring[(j & (RING - 1)) * RS] = 0xFFFFFFFFu;
 #pragma unroll
-      for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
-      active = true;
+        for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
+        active = true;
+      }
     }
+    // Warp-uniform tile sequence: the full 16-slot tiles every busy lane
+    // needs, then remainder tiles sized for the largest remainder in the warp.
+    // Lanes with narrower windows compute padding slots instead of taking a
+    // different branch.
+    const int n = busy ? je - js + 1 : 0;
+    const int full = (int)__reduce_min_sync(kFullMask, busy ? (unsigned)(n >> 4) : 0xFFFFFFFFu);
+    int rem = (int)__reduce_max_sync(kFullMask, busy ? (unsigned)(n - 16 * full) : 0u);
+    if (!busy) continue;
     const int cols = (i == nq - 1) ? lastcols : 32;
-    n_done += (unsigned long long)(je - js + 1) * cols;
+    n_done += (unsigned long long)n * cols;
     if (i + 1 < nq) {
 #pragma unroll
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
     }
-    uint32_t cw = 0;  // column carries entering the current tile
-    for (int base = js; base <= je; base += TW) {
-      uint32_t row[TW], pl[P][TW];
-      int zold = 0;
-#pragma unroll
-      for (int m = 0; m < TW; m++) {
-        const int j = base + m;
-        const bool in = j <= je;
-        row[m] = in ? ring[(j & (kRingBlocks - 1)) * RS] : 0u;
-        zold += in ? __popc(~row[m]) : 0;
-#pragma unroll
-        for (int p = 0; p < P; p++) pl[p][m] = in ? s_pl[j * P + p] : 0u;
+    {
+      uint32_t cw = 0, ncw = 0;
+      int base = js;
+      for (int t = 0; t < full; t++, base += 16) {
+        zw += tiled_tile<P, 16, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+        cw = ncw << (32 - cols);  // column 0's carry at bit 31
+        ncw = 0;
       }
-      uint32_t rv[P];
-#pragma unroll
-      for (int p = 0; p < P; p++) rv[p] = __brev(cur[p]);
-      uint32_t cin = cw, cout = 0;
-      for (int k = 0; k < cols; k++) {
-        uint32_t mk[P];
-#pragma unroll
-        for (int p = 0; p < P; p++) {
-          mk[p] = (uint32_t)((int)rv[p] >> 31);
-          rv[p] <<= 1;
-        }
-        uint32_t carry = cin & 1u;
-        cin >>= 1;
-        dp_tile_column<P, TW>(row, pl, mk, carry);
-        cout |= carry << k;
+      for (; rem > 12; rem -= 16, base += 16) {
+        zw += tiled_tile<P, 16, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+        cw = ncw << (32 - cols);
+        ncw = 0;
       }
-      int znew = 0;
-#pragma unroll
-      for (int m = 0; m < TW; m++) {
-        const int j = base + m;
-        if (j <= je) {
-          ring[(j & (kRingBlocks - 1)) * RS] = row[m];
-          znew += __popc(~row[m]);
-        }
-      }
-      zw += znew - zold;
-      cw = cout;
+      if (rem > 8)
+        zw += tiled_tile<P, 12, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+      else if (rem > 4)
+        zw += tiled_tile<P, 8, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+      else if (rem > 0)
+        zw += tiled_tile<P, 4, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
     }
     i++;
     bool finished = i >= nq;
     if (!finished) {
       if (i - B > 0) {  // block js leaves the band
-        const uint32_t r0 = ring[(js & (kRingBlocks - 1)) * RS];
+        const uint32_t r0 = ring[(js & (RING - 1)) * RS];
         frozen += __popc(~r0 & (js == nb1 - 1 ? vlast : 0xFFFFFFFFu));
         zw -= __popc(~r0);
         js++;
       }
       if (i + B <= nb1 - 1) {  // block je enters all-ones
         je++;
-        ring[(je & (kRingBlocks - 1)) * RS] = 0xFFFFFFFFu;
+        ring[(je & (RING - 1)) * RS] = 0xFFFFFFFFu;
       }
       if (js > je) finished = true;
     }
     if (finished) {
       int sum = frozen;
       for (int j = js; j <= je; j++)
-        sum += __popc(~ring[(j & (kRingBlocks - 1)) * RS] & (j == nb1 - 1 ? vlast : 0xFFFFFFFFu));
+        sum += __popc(~ring[(j & (RING - 1)) * RS] & (j == nb1 - 1 ? vlast : 0xFFFFFFFFu));
       finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, sum, cutoff, L2, net2, qpl, s_list, n_members);
       active = false;
       state = -1;
@@ -700,14 +609,16 @@ static AlignFn align_fn(int type, int cls) {
       case 1: return k_align_win<2, 16>;
       case 2: return k_align_win<2, 24>;
       case 3: return k_align_win<2, 32>;
-      case 4: return k_align_tiled<2>;
+      case 4: return k_align_tiled<2, 64>;
+      case 5: return k_align_tiled<2, 128>;
       default: return k_align_generic<2>;
     }
   }
   switch (cls) {
     case 0: return k_align_win<5, 8>;
     case 1: return k_align_win<5, 16>;
-    case 2: return k_align_tiled<5>;
+    case 2: return k_align_tiled<5, 64>;
+    case 3: return k_align_tiled<5, 128>;
     default: return k_align_generic<5>;
   }
 }
@@ -716,7 +627,7 @@ static AlignFn align_fn(int type, int cls) {
 static size_t align_smem(int type, int max_nb, int cls) {
   const int P = type ? 5 : 2;
   size_t words = (size_t)(((max_nb * P + 3) & ~3) + kListWords);
-  if (cls == tiled_class(type)) words += (size_t)kRingBlocks * kAlignThreads;
+  if (is_tiled_class(type, cls)) words += (size_t)class_cap(type, cls) * kAlignThreads;
   return 4u * words;
 }
 

@@ -62,7 +62,11 @@ int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond) 
       CK(cudaStreamWaitEvent(c->stream, c->join_ev[k], 0));
     }
   } else {
-    for (int k = 0; k < nc; k++) CK(ngia::launch_align(c, k, c->stream, 0));
+    for (int k = 0; k < nc; k++) {
+      if (prof) CK(cudaEventRecord(c->ev_cls[k], c->stream));
+      CK(ngia::launch_align(c, k, c->stream, 0));
+    }
+    if (prof) CK(cudaEventRecord(c->ev_cls[nc], c->stream));
   }
   if (prof) CK(cudaEventRecord(c->ev_p2, c->stream));
   CK(ngia::launch_next(c, (unsigned long long)cond, graph ? 1 : 0));
@@ -74,6 +78,10 @@ void account_stages(ngia_ctx *c) {
   float a = 0.f, b = 0.f;
   if (cudaEventElapsedTime(&a, c->ev_p0, c->ev_p1) == cudaSuccess) c->ms_filter += a;
   if (cudaEventElapsedTime(&b, c->ev_p1, c->ev_p2) == cudaSuccess) c->ms_align += b;
+  for (int k = 0; k < ngia::num_classes(c->db.type); k++) {
+    float m = 0.f;
+    if (cudaEventElapsedTime(&m, c->ev_cls[k], c->ev_cls[k + 1]) == cudaSuccess) c->ms_class[k] += m;
+  }
 }
 
 void fill_stats(const ngia_ctx *c, ngia_stats *stats) {
@@ -89,6 +97,10 @@ void fill_stats(const ngia_ctx *c, ngia_stats *stats) {
   stats->done_cells = (int64_t)s.st_done_cells;
   stats->ms_filter = c->ms_filter;
   stats->ms_align = c->ms_align;
+  for (int k = 0; k < 8; k++) {
+    stats->class_pairs[k] = k < ngia::kNumClasses ? (int64_t)s.st_class_pairs[k] : 0;
+    stats->class_ms[k] = k < ngia::kNumClasses ? c->ms_class[k] : 0.0;
+  }
 }
 
 void destroy_graph(ngia_ctx *c) {
@@ -171,6 +183,8 @@ extern "C" int ngia_open(const ngia_db_view *v, ngia_ctx **out) {
       cudaEventCreate(&c->ev_p0) != cudaSuccess || cudaEventCreate(&c->ev_p1) != cudaSuccess ||
       cudaEventCreate(&c->ev_p2) != cudaSuccess)
     return bail(fail(NGIA_E_CUDA, "cannot create event"));
+  for (auto &ev : c->ev_cls)
+    if (cudaEventCreate(&ev) != cudaSuccess) return bail(fail(NGIA_E_CUDA, "cannot create event"));
   const int64_t n = v->n;
   const int type = v->type;
   const int A = ngia::count_words(type);
@@ -270,6 +284,8 @@ extern "C" int ngia_close(ngia_ctx *c) {
   if (c->fork_ev) cudaEventDestroy(c->fork_ev);
   for (cudaEvent_t ev : {c->ev_step0, c->ev_step1, c->ev_p0, c->ev_p1, c->ev_p2})
     if (ev) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : c->ev_cls)
+    if (ev) cudaEventDestroy(ev);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return NGIA_OK;
@@ -299,6 +315,7 @@ extern "C" int ngia_cluster_begin(ngia_ctx *c, const ngia_params *p, int32_t mod
   if (c->db.has_short && !c->prm.precise) c->prm.word_order = 1;  // exact path is word first
   c->mode = mode;
   c->ms_filter = c->ms_align = 0.0;
+  for (double &m : c->ms_class) m = 0.0;
   c->last_step_ms = 0.f;
   CK(ngia::launch_init_run(c));
   rc = pull_state(c);

@@ -8,7 +8,7 @@
 
 namespace ngia {
 
-constexpr int kFullMask = -1;
+constexpr unsigned kFullMask = 0xFFFFFFFFu;
 constexpr int kMaxLenDev = 65536;              // makeDB keeps records <= 65,536
 constexpr int kMaxBlocks = kMaxLenDev / 32;    // 2048 plane blocks
 constexpr int kListWords = 2048;               // rep k-mer presence bitset (65,536 bits)
@@ -17,23 +17,25 @@ constexpr int kRefGridThreads = 128 * 128;     // BLOCK*WARP of the reference la
 // Alignment work classes.  Pairs are queued by the width A of their active
 // band window (rep blocks touched by one query block, min(2B+1, nb1)).  The
 // register-window classes hold the whole window in registers (capacity WC);
-// the tiled class keeps up to kRingBlocks window rows per pair in shared
-// memory and streams them through 16-slot register tiles; the last class of
-// each type is the generic kernel (any width).
-constexpr int kNumClasses = 6;
-constexpr int kRingBlocks = 128;
+// the tiled classes keep up to 64 or 128 window rows per pair in a
+// shared-memory ring and stream them through 16-slot register tiles; the last
+// class of each type is the generic kernel (any width).
+constexpr int kNumClasses = 7;
+constexpr int kRingBlocks = 128;  // largest ring (the tiled classes use 64 and 128)
 __host__ __device__ inline int class_cap(int type, int c) {
-  // DNA: 8,16,24,32 | tiled 128 | generic;  protein: 8,16 | tiled 128 | generic
+  // DNA: 8,16,24,32 | tiled 64, 128 | generic;  protein: 8,16 | tiled 64, 128 | generic
   if (type == 0) {
-    const int caps[6] = {8, 16, 24, 32, kRingBlocks, 0};
+    const int caps[7] = {8, 16, 24, 32, 64, 128, 0};
     return caps[c];
   }
-  const int caps[6] = {8, 16, kRingBlocks, 0, 0, 0};
+  const int caps[7] = {8, 16, 64, 128, 0, 0, 0};
   return caps[c];
 }
-__host__ __device__ inline int num_classes(int type) { return type == 0 ? 6 : 4; }
-__host__ __device__ inline int tiled_class(int type) { return num_classes(type) - 2; }
+__host__ __device__ inline int num_classes(int type) { return type == 0 ? 7 : 5; }
 __host__ __device__ inline int generic_class(int type) { return num_classes(type) - 1; }
+__host__ __device__ inline bool is_tiled_class(int type, int c) {
+  return c == generic_class(type) - 1 || c == generic_class(type) - 2;
+}
 __host__ __device__ inline int class_of(int type, int A) {
   const int g = generic_class(type);
   for (int c = 0; c < g; c++)
@@ -72,6 +74,7 @@ struct RunState {
   unsigned long long st_candidates, st_base_pass, st_align_pairs, st_members;
   unsigned long long st_band_cells, st_filter_bytes, st_word_checks, st_word_pass;
   unsigned long long st_done_cells;  // in-band cells actually computed
+  unsigned long long st_class_pairs[kNumClasses];
 };
 
 // Run parameters (constant during one clustering).

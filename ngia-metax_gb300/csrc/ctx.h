@@ -36,8 +36,9 @@ struct ngia_ctx {
   cudaEvent_t fork_ev = nullptr, join_ev[ngia::kNumClasses] = {nullptr};
   // timing: whole steps, and (profiling, plain form) filter / align stages
   cudaEvent_t ev_step0 = nullptr, ev_step1 = nullptr, ev_p0 = nullptr, ev_p1 = nullptr, ev_p2 = nullptr;
+  cudaEvent_t ev_cls[ngia::kNumClasses + 1] = {nullptr};
   bool profiling = false;
-  double ms_filter = 0.0, ms_align = 0.0;
+  double ms_filter = 0.0, ms_align = 0.0, ms_class[ngia::kNumClasses] = {0.0};
   float last_step_ms = 0.f;
 };
 

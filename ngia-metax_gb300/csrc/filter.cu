@@ -91,6 +91,7 @@ __global__ void k_init_run(DevDB db, RunBufs rb, RunParams prm) {
     st->st_candidates = st->st_base_pass = st->st_align_pairs = st->st_members = 0;
     st->st_band_cells = st->st_filter_bytes = st->st_word_checks = st->st_word_pass = 0;
     st->st_done_cells = 0;
+    for (int k = 0; k < kNumClasses; k++) st->st_class_pairs[k] = 0;
   }
 }
 
@@ -487,6 +488,7 @@ __global__ void k_next(DevDB db, RunBufs rb, unsigned long long cond, int use_co
   }
   if (threadIdx.x == 0) {
     st->iter += 1;
+    for (int k = 0; k < kNumClasses; k++) st->st_class_pairs[k] += st->qcount[k];
     if (s_found >= 0) {
       st->rep = s_found;
     } else {

@@ -49,11 +49,15 @@ class SynthParams(C.Structure):
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("iterations", "candidates", "base_pass", "align_pairs", "members",
                                          "band_cells", "filter_bytes", "word_checks", "done_cells")] + \
-        [("ms_filter", C.c_double), ("ms_align", C.c_double)]
+        [("ms_filter", C.c_double), ("ms_align", C.c_double), ("class_pairs", C.c_int64 * 8),
+         ("class_ms", C.c_double * 8)]
 
     def as_dict(self) -> dict:
-        return {n: (float(getattr(self, n)) if n.startswith("ms_") else int(getattr(self, n)))
-                for n, _ in self._fields_}
+        d = {}
+        for n, _ in self._fields_:
+            v = getattr(self, n)
+            d[n] = list(v) if n.startswith("class_") else (float(v) if n.startswith("ms_") else int(v))
+        return d
 
 
 _lib = None

@@ -44,6 +44,9 @@ def build_oracle() -> Path:
     exe = OUT / "ngia_oracle"
     if _stale(exe, src + hdr + [HERE / "oracle_main.c"]):
         _run([CC] + CFLAGS + [str(HERE / "oracle_main.c"), str(src[0]), "-o", str(exe), "-lm"])
+    nofma = OUT / "liboracle_nofma.so"  # separately rounded band shift (fixture search only)
+    if _stale(nofma, src + hdr):
+        _run([CC] + CFLAGS + ["-DORA_BAND_NOFMA", "-fPIC", "-shared", str(src[0]), "-o", str(nofma), "-lm"])
     return lib
 
 

@@ -145,8 +145,15 @@ int ora_dp_sum(const uint32_t *rep, const uint32_t *query, int type, float s, in
   const uint32_t *packed2 = query + hw;
   uint32_t line[2048];
   memset(line, 0xFF, sizeof(uint32_t) * (size_t)(netLen321 > 0 ? netLen321 : 1));
-  /* nvcc contracts (float)L1 - (float)L2 * s into one fused multiply-add */
+  /* nvcc contracts (float)L1 - (float)L2 * s into one fused multiply-add;
+   * ORA_BAND_NOFMA builds the separately rounded variant, used only to find
+   * inputs on which the two differ (tests/golden/make_golden.py). */
+#ifdef ORA_BAND_NOFMA
+  volatile float prod = (float)length2 * s;
+  int shift = (int)ceilf((float)length1 - prod);
+#else
   int shift = (int)ceilf(fmaf(-(float)length2, s, (float)length1));
+#endif
   shift = (shift + 31) / 32;
   if (band) *band = shift;
   int64_t ncell = 0;

@@ -17,14 +17,27 @@ STAT_NAMES = ["iterations", "candidates", "base_pass", "word_eval", "word_pass",
               "filter_bytes"]
 
 _lib = None
+_nofma = None
 
 
-def lib() -> C.CDLL:
-    global _lib
+def lib(nofma: bool = False) -> C.CDLL:
+    """The oracle library; nofma=True gives the separately rounded band-shift
+    variant used only to search for inputs that tell the two apart."""
+    global _lib, _nofma
+    if nofma:
+        if _nofma is None:
+            _nofma = _load(HERE / "_build" / "liboracle_nofma.so")
+        return _nofma
     if _lib is None:
-        if not LIB.exists():
-            raise ImportError(f"{LIB} is missing: build it with oracle/build_oracle.py")
-        L = C.CDLL(str(LIB))
+        _lib = _load(LIB)
+    return _lib
+
+
+def _load(path: Path) -> C.CDLL:
+    if True:
+        if not path.exists():
+            raise ImportError(f"{path} is missing: build it with oracle/build_oracle.py")
+        L = C.CDLL(str(path))
         P = C.POINTER
         L.ora_cluster.restype = C.c_int64
         L.ora_cluster.argtypes = [P(C.c_uint32), P(C.c_int64), C.c_int, C.c_int, C.c_float, C.c_int, C.c_int,
@@ -36,8 +49,7 @@ def lib() -> C.CDLL:
         L.ora_clamp.argtypes = [C.c_int, P(C.c_float), P(C.c_int), P(C.c_int)]
         L.ora_dp_sum.restype = C.c_int
         L.ora_dp_sum.argtypes = [P(C.c_uint32), P(C.c_uint32), C.c_int, C.c_float, P(C.c_int), P(C.c_int64)]
-        _lib = L
-    return _lib
+    return L
 
 
 def clamp(db_type: int, s: float, w: int, precise: int = 0):
@@ -47,7 +59,7 @@ def clamp(db_type: int, s: float, w: int, precise: int = 0):
 
 
 def cluster(words: np.ndarray, rec_off: np.ndarray, db_type: int, s: float, w: int, precise: int = 0,
-            threads: int = 0, max_iters: int = 0):
+            threads: int = 0, max_iters: int = 0, nofma: bool = False):
     """Clusters with already-clamped parameters; returns (cluster, identity, stats)."""
     words = np.ascontiguousarray(words, dtype=np.uint32)
     rec_off = np.ascontiguousarray(rec_off, dtype=np.int64)
@@ -55,7 +67,7 @@ def cluster(words: np.ndarray, rec_off: np.ndarray, db_type: int, s: float, w: i
     cl = np.empty(n, dtype=np.int32)
     ident = np.empty(n, dtype=np.int32)
     st = np.zeros(NSTATS, dtype=np.int64)
-    lib().ora_cluster(words.ctypes.data_as(C.POINTER(C.c_uint32)), rec_off.ctypes.data_as(C.POINTER(C.c_int64)),
+    lib(nofma).ora_cluster(words.ctypes.data_as(C.POINTER(C.c_uint32)), rec_off.ctypes.data_as(C.POINTER(C.c_int64)),
                       n, db_type, C.c_float(s), w, precise, threads, max_iters,
                       cl.ctypes.data_as(C.POINTER(C.c_int32)), ident.ctypes.data_as(C.POINTER(C.c_int32)),
                       st.ctypes.data_as(C.POINTER(C.c_int64)))

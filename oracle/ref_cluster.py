@@ -7,6 +7,9 @@ produce golden outputs.  Test infrastructure.
 `stage` copies the program's five source files (cluster.cpp, func.cu,
 func.h, cmdline.h, timer.h) unchanged into baseline/_ref/signalNode/ — the
 git-ignored directory that carries the reference install to GPU hosts.
+`compare OUTDIR --workload W` runs the reference and the drop-in `cluster`
+on one generated workload, times both and byte-compares their outputs.
+
 `run` compiles them there with nvcc for sm_103a exactly as the reference
 Makefile line does (nvcc src/cluster.cpp src/func.cu -o cluster), adding only
 -gencode and `-include oracle/ref_copykind.h`, builds each golden fixture's
@@ -85,8 +88,62 @@ def run(outdir: str) -> None:
     print(json.dumps(report, indent=1))
 
 
+def compare(outdir: str, workload: str, similarity: float, word: int, n_seqs: int = 0, seed: int = 1,
+            timeout: int = 1200) -> dict:
+    """Generates a workload, runs the reference `cluster` and the drop-in
+    `cluster` on the same database, times both (wall clock, including their
+    own database loading and result writing) and byte-compares the outputs."""
+    sys.path.insert(0, str(ROOT / "ngia-metax_gb300"))
+    import ngia
+
+    exe = build()
+    out = Path(outdir)
+    dbdir, o_ref, o_new = out / "db", out / "ref", out / "ours"
+    for d in (dbdir, o_ref, o_new):
+        d.mkdir(parents=True, exist_ok=True)
+    cfg = dict(ngia.CONFIGS[workload])
+    if n_seqs:
+        cfg["n_seqs"] = n_seqs
+    seqs = ngia.synth(**cfg, seed=seed)
+    ngia.write_fasta(str(dbdir / "in.fasta"), seqs, seqs.off, width=80)
+    seqs.close()
+    ngia.makedb(str(dbdir / "in.fasta"), str(dbdir), cfg["type"])
+    args = ["-i", str(dbdir), "-w", str(word), "-s", str(similarity)]
+    res = {"workload": workload, "n_seqs": cfg["n_seqs"], "similarity": similarity, "word": word}
+    for name, cmd, od in (("reference", [str(exe)], o_ref),
+                          ("ours", [str(ROOT / "ngia-metax_gb300" / "_build" / "cluster")], o_new)):
+        t0 = time.time()
+        try:
+            r = subprocess.run(cmd + args + ["-o", str(od)], capture_output=True, text=True, timeout=timeout)
+            res[name] = {"rc": r.returncode, "seconds": round(time.time() - t0, 3),
+                         "clusters": next((ln.split("\t")[1] for ln in r.stdout.splitlines()
+                                           if ln.startswith("Cluster:")), None)}
+        except subprocess.TimeoutExpired:
+            res[name] = {"rc": None, "seconds": timeout, "timeout": True}
+    same = all((o_ref / f).exists() and (o_ref / f).read_bytes() == (o_new / f).read_bytes()
+               for f in ("cluster.txt", "represent.fasta"))
+    res["outputs_identical"] = same
+    shutil.rmtree(dbdir, ignore_errors=True)
+    (out / "compare.json").write_text(json.dumps(res, indent=1) + "\n")
+    print(json.dumps(res))
+    return res
+
+
 if __name__ == "__main__":
     if sys.argv[1] == "stage":
         stage()
     elif sys.argv[1] == "run":
         run(sys.argv[2])
+    elif sys.argv[1] == "compare":
+        import argparse
+
+        ap = argparse.ArgumentParser()
+        ap.add_argument("cmd")
+        ap.add_argument("outdir")
+        ap.add_argument("--workload", default="dna_small")
+        ap.add_argument("--similarity", type=float, default=0.85)
+        ap.add_argument("--word", type=int, default=5)
+        ap.add_argument("--n-seqs", type=int, default=0)
+        ap.add_argument("--timeout", type=int, default=1200)
+        a = ap.parse_args()
+        compare(a.outdir, a.workload, a.similarity, a.word, a.n_seqs, timeout=a.timeout)
