@@ -215,6 +215,23 @@ int ngia_unpin_host(void *ptr);
  * alignment inner loop); *gops receives lane-operations per second / 1e9. */
 int ngia_measure_int_peak(double *gops);
 
+/* Banded-LCS scores of the representative record at d_words + rep_off
+ * against the n query records at d_words + d_query_off[k], written to
+ * d_scores[k]; all three arrays are device memory the caller owns, and the
+ * call allocates nothing.  It has no counterpart in the reference: it is for
+ * callers that cannot allocate device memory — applications whose device
+ * memory is owned by another allocator or pool, or loops that must not pay
+ * for cudaMalloc/cudaFree.  Working rows live in a fixed 4 MiB device array
+ * of this library (held by every GPU that loads it until the process exits),
+ * which limits the representative to 65,536 residues (NGIA_E_LIMIT beyond).
+ * The first call on a device looks the array up and must precede any stream
+ * capture; calls that overlap on the GPU share the array and race — serialise
+ * them.  Work is queued on `stream` (NULL = default stream); the scores are
+ * ready when it completes. */
+int ngia_rep_scores_noalloc(const uint32_t *d_words, int64_t rep_off,
+                            const int64_t *d_query_off, int32_t n, int32_t type,
+                            float similarity, int32_t *d_scores, void *stream);
+
 /* CUDA stream the context launches on (as an opaque handle, for timing). */
 void *ngia_stream(ngia_ctx *ctx);
 

@@ -99,6 +99,7 @@ def lib() -> C.CDLL:
         "ngia_cluster_stats": (C.c_int, [VP, P(Stats)]),
         "ngia_step_device_ms": (C.c_int, [VP, P(C.c_float)]),
         "ngia_set_profiling": (C.c_int, [VP, I32]),
+        "ngia_rep_scores_noalloc": (C.c_int, [VP, I64, VP, I32, I32, C.c_float, VP, VP]),
         "ngia_close": (C.c_int, [VP]),
     }
     for name, (res, args) in sig.items():
@@ -147,6 +148,14 @@ def pin_host(arr: np.ndarray) -> None:
 
 def unpin_host(arr: np.ndarray) -> None:
     _check(lib().ngia_unpin_host(arr.ctypes.data))
+
+
+def rep_scores_noalloc(d_words: int, rep_off: int, d_query_off: int, n: int, db_type: int, similarity: float,
+                       d_scores: int, stream: int = 0) -> None:
+    """Scores one representative against n queries; all pointers are device
+    addresses owned by the caller (the library allocates nothing)."""
+    _check(lib().ngia_rep_scores_noalloc(d_words, rep_off, d_query_off, n, db_type, similarity, d_scores,
+                                         stream or None))
 
 
 def params_clamp(db_type: int, similarity: float, word_length: int, precise: int = 0) -> Params:
