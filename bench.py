@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--cpu-only", action="store_true", help="no GPU at all (tests of the replica logic)")
+    ap.add_argument("--cpu-only", action="store_true",
+                    help="replica plumbing with the CPU oracle as the engine (tests; no GPU)")
     return ap.parse_args()
 
 
@@ -344,11 +345,42 @@ def run_cpu_baseline(args, db, p, cfg):
                       f" C/OpenMP restatement of the reference on all host threads"}
 
 
+def run_cpu_replicas(args, dist: Dist):
+    """Replica plumbing without a GPU (tests): every rank clusters its copy of
+    a small workload with the oracle for the timed steps; rank 0 reports the
+    summed work over the slowest rank's time, exactly as the GPU arm does."""
+    from oracle import oracle
+    import ngia
+
+    db, cfg = make_db(args)
+    p = ngia.params_clamp(cfg["type"], args.similarity, args.word, 0)
+    for _ in range(args.warmup):
+        oracle.cluster(db.words, db.rec_off, cfg["type"], p.similarity, p.word_length, p.precise, threads=1,
+                       max_iters=args.iters_per_step)
+    dist.barrier()
+    t0 = time.perf_counter()
+    cands = 0
+    for _ in range(args.steps):
+        _, _, st = oracle.cluster(db.words, db.rec_off, cfg["type"], p.similarity, p.word_length, p.precise,
+                                  threads=1, max_iters=args.iters_per_step)
+        cands += st["candidates"]
+    T = dist.reduce(time.perf_counter() - t0, "max")
+    total = dist.reduce(float(cands), "sum")
+    dist.barrier()
+    if dist.rank == 0:
+        print(json.dumps({"metric": METRIC, "value": total / T, "unit": UNIT, "n_gpus": dist.world,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
+                          "higher_is_better": True, "scaling": "weak", "cpu_only": True,
+                          "config": workload_desc(args, cfg)}), flush=True)
+
+
 def main():
     args = parse()
     dist = Dist()
     try:
-        if args.impl == "reference":
+        if args.cpu_only:
+            run_cpu_replicas(args, dist)
+        elif args.impl == "reference":
             run_reference(args, dist)
         else:
             run_ours(args, dist)

@@ -191,6 +191,27 @@ int ngia_step_device_ms(ngia_ctx *ctx, float *ms);
  * totals land in ngia_stats.ms_filter / ms_align). */
 int ngia_set_profiling(ngia_ctx *ctx, int32_t on);
 
+/* ---- batches of independent jobs ---------------------------------------- */
+typedef struct ngia_batch ngia_batch;
+
+/* Opens n_jobs independent clustering jobs (one database view each; each is
+ * copied to the device with grids sized to the job). */
+int ngia_batch_open(const ngia_db_view *jobs, int32_t n_jobs, ngia_batch **out);
+
+/* Clusters every job with its own parameters (params[j], clamped).
+ * NGIA_MODE_GRAPH: all jobs in one CUDA graph launch — one conditional while
+ * node per job, no host round trip until the whole batch is done;
+ * NGIA_MODE_PLAIN: the jobs one after the other with the host-loop driver.
+ * max_iters > 0 stops each job after that many representatives (sampling).
+ * cluster_out[j] / identity_out[j] (either may be NULL) receive job j's
+ * arrays (jobs[j].n entries); stats (may be NULL) the sums over jobs.
+ * Results are identical to clustering every job alone. */
+int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t mode,
+                   int64_t max_iters, int32_t **cluster_out,
+                   int32_t **identity_out, ngia_stats *stats);
+
+int ngia_batch_close(ngia_batch *b);
+
 /* Per-pair stage values for (rep, cands[k]) pairs, for unit-level parity:
  * out[4k+0] = composition sum, out[4k+1] = short-word count (-1 when the
  * reference skips it because a net length is < 16), out[4k+2] = banded-LCS

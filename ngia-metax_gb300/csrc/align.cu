@@ -34,6 +34,7 @@
 // Accepted pairs are always computed to the end (their score is reported).
 #include <climits>
 #include <cstdlib>
+#include <mutex>
 
 #include "ctx.h"
 #include "dp_asm.cuh"
@@ -631,12 +632,25 @@ static size_t align_smem(int type, int max_nb, int cls) {
   return 4u * words;
 }
 
+// The dynamic shared memory limit is a property of the kernel on a device, not
+// of a context: it only ever grows, so that a context opened on a database of
+// shorter records cannot lower it beneath the launches of an open context on
+// longer ones.
 cudaError_t align_configure(int type, int max_nb) {
+  static std::mutex mu;
+  static int configured[64][2][kNumClasses] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
   for (int c = 0; c < num_classes(type); c++) {
-    cudaError_t e = cudaFuncSetAttribute((const void *)align_fn(type, c),
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)align_smem(type, max_nb, c));
+    const int want = (int)align_smem(type, max_nb, c);
+    int &have = configured[dev][type ? 1 : 0][c];
+    if (want <= have) continue;
+    e = cudaFuncSetAttribute((const void *)align_fn(type, c), cudaFuncAttributeMaxDynamicSharedMemorySize, want);
     if (e != cudaSuccess) return e;
+    have = want;
   }
   return cudaSuccess;
 }

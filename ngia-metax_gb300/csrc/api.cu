@@ -9,6 +9,7 @@
 //   ngia_close           finish (767-781)
 #include <algorithm>
 #include <climits>
+#include <cstdio>
 #include <cstring>
 #include <new>
 
@@ -16,6 +17,7 @@
 #include "ctx.h"
 
 using ngia::fail;
+using namespace ngia::drv;
 
 #define CK(call)                                                                                  \
   do {                                                                                            \
@@ -23,7 +25,8 @@ using ngia::fail;
     if (e_ != cudaSuccess) return fail(NGIA_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_));     \
   } while (0)
 
-namespace {
+namespace ngia {
+namespace drv {
 
 template <class T>
 cudaError_t dalloc(T **p, size_t count) {
@@ -45,6 +48,8 @@ int pull_state(ngia_ctx *c) {
 
 // One greedy iteration: prepare the representative, filter the unclustered
 // set into class queues, align every class, pick the next representative.
+// In graph form the class kernels of a single job run as parallel branches;
+// batch members keep them on one stream (the batch runs jobs side by side).
 int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond) {
   const bool prof = c->profiling && !graph;
   if (prof) CK(cudaEventRecord(c->ev_p0, c->stream));
@@ -52,7 +57,7 @@ int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond) 
   CK(ngia::launch_filter(c));
   if (prof) CK(cudaEventRecord(c->ev_p1, c->stream));
   const int nc = ngia::num_classes(c->db.type);
-  if (graph) {
+  if (graph && !c->batch_member) {
     // classes run as parallel branches of the body graph
     CK(cudaEventRecord(c->fork_ev, c->stream));
     for (int k = 0; k < nc; k++) {
@@ -129,9 +134,17 @@ int build_graph(ngia_ctx *c) {
   int rc = enqueue_iteration(c, true, cond);
   cudaGraph_t captured = nullptr;
   cudaError_t e = cudaStreamEndCapture(c->stream, &captured);
-  if (rc != NGIA_OK) return rc;
-  if (e != cudaSuccess) return fail(NGIA_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
-  CK(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
+  if (rc != NGIA_OK || e != cudaSuccess) {
+    destroy_graph(c);  // a body whose capture failed is never instantiated
+    return rc != NGIA_OK ? rc : fail(NGIA_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  }
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, c->graph, 0);
+  if (e != cudaSuccess) {
+    destroy_graph(c);
+    return fail(NGIA_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+  }
+  c->graph_exec = exec;
   c->graph_ready = true;
   c->graph_prm = c->prm;
   return NGIA_OK;
@@ -152,15 +165,19 @@ int validate_params(int type, const ngia_params *p) {
   return NGIA_OK;
 }
 
-}  // namespace
+}  // namespace drv
+}  // namespace ngia
 
-extern "C" int ngia_open(const ngia_db_view *v, ngia_ctx **out) {
+extern "C" int ngia_open(const ngia_db_view *v, ngia_ctx **out) { return ngia::drv::open_ctx(v, false, out); }
+
+int ngia::drv::open_ctx(const ngia_db_view *v, bool batch_member, ngia_ctx **out) {
   ngia::clear_error();
   if (!v || !out) return fail(NGIA_E_ARG, "ngia_open: null argument");
   if (v->n <= 0 || (v->type != 0 && v->type != 1) || !v->words || !v->rec_off || v->n_words <= 0)
     return fail(NGIA_E_ARG, "ngia_open: empty or malformed database view (n=%d type=%d)", v->n, v->type);
   ngia_ctx *c = new (std::nothrow) ngia_ctx();
   if (!c) return fail(NGIA_E_NOMEM, "ngia_open: out of host memory");
+  c->batch_member = batch_member;
   *out = nullptr;
   int rc = NGIA_OK;
   auto bail = [&](int r) {
@@ -240,6 +257,13 @@ extern "C" int ngia_open(const ngia_db_view *v, ngia_ctx **out) {
   for (int k = 0; k < ngia::num_classes(type); k++)
     c->grid_align[k] = c->num_sms * ngia::align_occupancy(type, k, c->db.max_nb);
   c->grid_filter = c->num_sms * 8;
+  if (batch_member) {
+    // a batch runs many jobs side by side: size each job's grids to its own
+    // sequence count (one CTA per 128 candidates, one warp per bitmap word)
+    const int by_n = (int)std::min<int64_t>((n + 127) / 128, INT32_MAX);
+    for (int k = 0; k < ngia::num_classes(type); k++) c->grid_align[k] = std::max(1, std::min(c->grid_align[k], by_n));
+    c->grid_filter = std::max(1, std::min(c->grid_filter, (int)((nbw + 7) / 8)));
+  }
   const int g = ngia::generic_class(type);
   rb.generic_lanes = c->grid_align[g] * ngia::align_threads();
   rb.scratch_words = (int64_t)rb.generic_lanes * c->db.max_nb;

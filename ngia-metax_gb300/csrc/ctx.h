@@ -38,11 +38,20 @@ struct ngia_ctx {
   cudaEvent_t ev_step0 = nullptr, ev_step1 = nullptr, ev_p0 = nullptr, ev_p1 = nullptr, ev_p2 = nullptr;
   cudaEvent_t ev_cls[ngia::kNumClasses + 1] = {nullptr};
   bool profiling = false;
+  bool batch_member = false;  // grids sized to the job; serial class launches
   double ms_filter = 0.0, ms_align = 0.0, ms_class[ngia::kNumClasses] = {0.0};
   float last_step_ms = 0.f;
 };
 
 namespace ngia {
+// api.cu: driver internals shared with batch.cu / serve.cu
+namespace drv {
+int open_ctx(const ngia_db_view *v, bool batch_member, ngia_ctx **out);
+int pull_state(ngia_ctx *c);
+int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond);
+void fill_stats(const ngia_ctx *c, ngia_stats *stats);
+int validate_params(int type, const ngia_params *p);
+}  // namespace drv
 // loader.cu / filter.cu
 cudaError_t launch_loader(ngia_ctx *c, int32_t *d_maxnb, int32_t *d_short, int32_t *d_bad);
 cudaError_t launch_init_run(ngia_ctx *c);

@@ -100,6 +100,9 @@ def lib() -> C.CDLL:
         "ngia_step_device_ms": (C.c_int, [VP, P(C.c_float)]),
         "ngia_set_profiling": (C.c_int, [VP, I32]),
         "ngia_rep_scores_noalloc": (C.c_int, [VP, I64, VP, I32, I32, C.c_float, VP, VP]),
+        "ngia_batch_open": (C.c_int, [P(DBView), I32, P(VP)]),
+        "ngia_batch_run": (C.c_int, [VP, P(Params), I32, I64, P(P(I32)), P(P(I32)), P(Stats)]),
+        "ngia_batch_close": (C.c_int, [VP]),
         "ngia_close": (C.c_int, [VP]),
     }
     for name, (res, args) in sig.items():
@@ -374,6 +377,45 @@ class Context:
     def close(self) -> None:
         if self._h:
             lib().ngia_close(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Independent clustering jobs run side by side (ngia_batch_*)."""
+
+    def __init__(self, dbs: list):
+        self.dbs = list(dbs)
+        views = (DBView * len(self.dbs))(*[d.view for d in self.dbs])
+        self._h = C.c_void_p()
+        _check(lib().ngia_batch_open(views, len(self.dbs), C.byref(self._h)))
+
+    def run(self, params: list, mode: int = MODE_GRAPH, max_iters: int = 0):
+        """Returns ([cluster arrays], [identity arrays], summed stats)."""
+        n = len(self.dbs)
+        ps = (Params * n)(*params)
+        cls = [np.empty(d.n, dtype=np.int32) for d in self.dbs]
+        ids = [np.empty(d.n, dtype=np.int32) for d in self.dbs]
+        cptr = (C.POINTER(C.c_int32) * n)(*[_i32p(a) for a in cls])
+        iptr = (C.POINTER(C.c_int32) * n)(*[_i32p(a) for a in ids])
+        st = Stats()
+        _check(lib().ngia_batch_run(self._h, ps, mode, max_iters, cptr, iptr, C.byref(st)))
+        return cls, ids, st.as_dict()
+
+    def close(self) -> None:
+        if self._h:
+            lib().ngia_batch_close(self._h)
             self._h = C.c_void_p()
 
     def __enter__(self):
