@@ -372,6 +372,22 @@ __device__ __forceinline__ int tiled_tile(uint32_t *ring, const uint32_t *s_pl, 
   return znew - zold;
 }
 
+// The last tile of a block row, exactly `rem` (1..15, warp-uniform) slots wide.
+template <int P, int RING>
+__device__ __forceinline__ int tiled_rem(int rem, uint32_t *ring, const uint32_t *s_pl, int base, int je, int cols,
+                                         const uint32_t (&cur)[P], uint32_t &cw, uint32_t &ncw) {
+  switch (rem) {
+#define NGIA_REM(W) \
+  case W:           \
+    return tiled_tile<P, W, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+    NGIA_REM(1) NGIA_REM(2) NGIA_REM(3) NGIA_REM(4) NGIA_REM(5) NGIA_REM(6) NGIA_REM(7) NGIA_REM(8)
+    NGIA_REM(9) NGIA_REM(10) NGIA_REM(11) NGIA_REM(12) NGIA_REM(13) NGIA_REM(14) NGIA_REM(15)
+#undef NGIA_REM
+    default:
+      return 0;
+  }
+}
+
 // Tiled window: windows of up to RING rep blocks.  Each lane keeps its
 // pair's band rows in a shared-memory ring indexed by absolute rep block
 // (ring[(j mod RING) * threads + tid], so the 32 lanes of a warp hit 32
@@ -405,7 +421,13 @@ __global__ void __launch_bounds__(kAlignThreads, P == 2 ? (RING <= 64 ? 4 : 3) :
   uint32_t cur[P], nxt[P];
   unsigned long long n_pairs = 0, n_members = 0, n_cells = 0, n_done = 0;
   for (;;) {
-    claim(st, cls, h.qn, lane, state);
+    // A warp refills once prm.refill of its lanes are idle (or none is busy).
+    // Queue entries next to each other are candidates of similar length, so
+    // lanes that start together keep equal band windows block after block.
+    {
+      const unsigned idle = __ballot_sync(kFullMask, state == -1);
+      if (__popc(idle) >= prm.refill || !__any_sync(kFullMask, state >= 0)) claim(st, cls, h.qn, lane, state);
+    }
     if (__all_sync(kFullMask, state == -2)) break;
     // No lane leaves the loop body early: the warp-wide reductions below are
     // executed by all 32 lanes (lanes without a pair contribute neutral values).
@@ -462,17 +484,12 @@ __global__ void __launch_bounds__(kAlignThreads, P == 2 ? (RING <= 64 ? 4 : 3) :
         cw = ncw << (32 - cols);  // column 0's carry at bit 31
         ncw = 0;
       }
-      for (; rem > 12; rem -= 16, base += 16) {
+      for (; rem >= 16; rem -= 16, base += 16) {
         zw += tiled_tile<P, 16, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
         cw = ncw << (32 - cols);
         ncw = 0;
       }
-      if (rem > 8)
-        zw += tiled_tile<P, 12, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
-      else if (rem > 4)
-        zw += tiled_tile<P, 8, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
-      else if (rem > 0)
-        zw += tiled_tile<P, 4, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+      if (rem > 0) zw += tiled_rem<P, RING>(rem, ring, s_pl, base, je, cols, cur, cw, ncw);
     }
     i++;
     bool finished = i >= nq;

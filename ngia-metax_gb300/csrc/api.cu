@@ -151,7 +151,7 @@ int build_graph(ngia_ctx *c) {
 }
 
 bool same_params(const ngia::RunParams &a, const ngia::RunParams &b) {
-  return a.s == b.s && a.w == b.w && a.precise == b.precise && a.word_order == b.word_order;
+  return a.s == b.s && a.w == b.w && a.precise == b.precise && a.word_order == b.word_order && a.refill == b.refill;
 }
 
 int validate_params(int type, const ngia_params *p) {
@@ -336,6 +336,8 @@ extern "C" int ngia_cluster_begin(ngia_ctx *c, const ngia_params *p, int32_t mod
   c->prm.precise = p->precise;
   c->prm.word_order = 0;
   if (const char *wo = getenv("NGIA_WORD_ORDER")) c->prm.word_order = atoi(wo);
+  c->prm.refill = 32;
+  if (const char *rf = getenv("NGIA_REFILL")) c->prm.refill = std::max(1, std::min(32, atoi(rf)));
   if (c->db.has_short && !c->prm.precise) c->prm.word_order = 1;  // exact path is word first
   c->mode = mode;
   c->ms_filter = c->ms_align = 0.0;
@@ -463,6 +465,7 @@ extern "C" int ngia_pair_scores(ngia_ctx *c, const ngia_params *p, int32_t rep, 
   c->prm.s = p->similarity;
   c->prm.w = p->word_length;
   c->prm.precise = p->precise;
+  c->prm.refill = 32;
   int32_t *d_c = nullptr, *d_o = nullptr;
   CK(dalloc(&d_c, (size_t)n));
   CK(dalloc(&d_o, 4 * (size_t)n));

@@ -83,6 +83,7 @@ struct RunParams {
   int32_t w;
   int32_t precise;
   int32_t word_order;     // 0 auto, 1 word first, 2 alignment first
+  int32_t refill;         // tiled alignment: idle lanes a warp waits for before it claims new pairs
 };
 
 // Device buffers of one clustering run.
