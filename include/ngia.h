@@ -150,7 +150,7 @@ typedef struct ngia_stats {
     int64_t word_checks;   /* pairs the short-word filter was evaluated on   */
     int64_t done_cells;    /* in-band cells the alignment kernels computed   */
                            /* (fewer than band_cells: early rejection)       */
-    double  ms_filter;     /* device time of prep + filter launches and      */
+    double  ms_filter;     /* device time of the filter launches and         */
     double  ms_align;      /* of the alignment launches (profiling, plain)   */
     int64_t class_pairs[8];   /* pairs queued per alignment work class       */
     double  class_ms[8];      /* device time per class (profiling, plain)    */

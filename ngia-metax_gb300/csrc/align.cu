@@ -39,6 +39,18 @@
 #include "ctx.h"
 #include "dp_asm.cuh"
 
+// Build-time tuning of the tiled kernel: NGIA_TILED_MAIN_DNA and
+// NGIA_TILED_BLOCKS_DNA set the DNA main tile width and the resident CTAs per
+// SM requested from the register allocator.  On GB300 (1M DNA, s=0.85) 16
+// slots at 4 CTAs ran fastest: 24 slots (3 or 2 CTAs) and 32 slots (2 CTAs)
+// were 15-45% slower.
+#ifndef NGIA_TILED_MAIN_DNA
+#define NGIA_TILED_MAIN_DNA 16
+#endif
+#ifndef NGIA_TILED_BLOCKS_DNA
+#define NGIA_TILED_BLOCKS_DNA 4
+#endif
+
 namespace ngia {
 
 constexpr int kRepPlanesOff = 32;  // planes offset inside rb.rep_rec (filter.cu)
@@ -372,16 +384,19 @@ __device__ __forceinline__ int tiled_tile(uint32_t *ring, const uint32_t *s_pl, 
   return znew - zold;
 }
 
-// The last tile of a block row, exactly `rem` (1..15, warp-uniform) slots wide.
-template <int P, int RING>
+// The last tile of a block row, exactly `rem` (1..MT-1, warp-uniform) slots wide.
+template <int P, int RING, int MT>
 __device__ __forceinline__ int tiled_rem(int rem, uint32_t *ring, const uint32_t *s_pl, int base, int je, int cols,
                                          const uint32_t (&cur)[P], uint32_t &cw, uint32_t &ncw) {
   switch (rem) {
 #define NGIA_REM(W) \
   case W:           \
-    return tiled_tile<P, W, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+    if (W < MT) return tiled_tile<P, (W < MT ? W : 1), RING>(ring, s_pl, base, je, cols, cur, cw, ncw); \
+    return 0;
     NGIA_REM(1) NGIA_REM(2) NGIA_REM(3) NGIA_REM(4) NGIA_REM(5) NGIA_REM(6) NGIA_REM(7) NGIA_REM(8)
-    NGIA_REM(9) NGIA_REM(10) NGIA_REM(11) NGIA_REM(12) NGIA_REM(13) NGIA_REM(14) NGIA_REM(15)
+    NGIA_REM(9) NGIA_REM(10) NGIA_REM(11) NGIA_REM(12) NGIA_REM(13) NGIA_REM(14) NGIA_REM(15) NGIA_REM(16)
+    NGIA_REM(17) NGIA_REM(18) NGIA_REM(19) NGIA_REM(20) NGIA_REM(21) NGIA_REM(22) NGIA_REM(23) NGIA_REM(24)
+    NGIA_REM(25) NGIA_REM(26) NGIA_REM(27) NGIA_REM(28) NGIA_REM(29) NGIA_REM(30) NGIA_REM(31)
 #undef NGIA_REM
     default:
       return 0;
@@ -393,12 +408,18 @@ __device__ __forceinline__ int tiled_rem(int rem, uint32_t *ring, const uint32_t
 // (ring[(j mod RING) * threads + tid], so the 32 lanes of a warp hit 32
 // distinct banks whatever their j), and runs each query block tile by tile in
 // ascending rep-block order, all residues of the block per tile — the
-// reference's (i, j, k) loop order at tile granularity.  Full tiles are 16
-// slots; the remainder runs as a 4, 8, 12 or 16-slot tile (at most 3 padding
-// slots); the column carries pass between tiles in one word (one instruction
-// to pop a carry, one to push it).
+// reference's (i, j, k) loop order at tile granularity.  Full tiles are MT
+// slots (tiled_main); the remainder runs as one tile of exactly its width;
+// the column carries pass between tiles in one word (one instruction to pop a
+// carry, one to push it).  A warp's lanes start their pairs together (see the
+// refill below), so their windows are equally wide and padding is rare.
+//
+// Main tile width of the tiled kernel (16 slots; NGIA_TILED_MAIN_DNA for DNA).
+__host__ __device__ constexpr int tiled_main(int P) { return P == 2 ? NGIA_TILED_MAIN_DNA : 16; }
+__host__ __device__ constexpr int tiled_min_blocks(int P) { return P == 2 ? NGIA_TILED_BLOCKS_DNA : 2; }
+
 template <int P, int RING>
-__global__ void __launch_bounds__(kAlignThreads, P == 2 ? (RING <= 64 ? 4 : 3) : 2)
+__global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
     k_align_tiled(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode) {
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
@@ -462,13 +483,14 @@ __global__ void __launch_bounds__(kAlignThreads, P == 2 ? (RING <= 64 ? 4 : 3) :
         active = true;
       }
     }
-    // Warp-uniform tile sequence: the full 16-slot tiles every busy lane
-    // needs, then remainder tiles sized for the largest remainder in the warp.
+    // Warp-uniform tile sequence: the full MT-slot tiles every busy lane
+    // needs, then tiles sized for the largest remainder in the warp.
     // Lanes with narrower windows compute padding slots instead of taking a
     // different branch.
     const int n = busy ? je - js + 1 : 0;
-    const int full = (int)__reduce_min_sync(kFullMask, busy ? (unsigned)(n >> 4) : 0xFFFFFFFFu);
-    int rem = (int)__reduce_max_sync(kFullMask, busy ? (unsigned)(n - 16 * full) : 0u);
+    constexpr int MT = tiled_main(P);
+    const int full = (int)__reduce_min_sync(kFullMask, busy ? (unsigned)(n / MT) : 0xFFFFFFFFu);
+    int rem = (int)__reduce_max_sync(kFullMask, busy ? (unsigned)(n - MT * full) : 0u);
     if (!busy) continue;
     const int cols = (i == nq - 1) ? lastcols : 32;
     n_done += (unsigned long long)n * cols;
@@ -479,17 +501,17 @@ __global__ void __launch_bounds__(kAlignThreads, P == 2 ? (RING <= 64 ? 4 : 3) :
     {
       uint32_t cw = 0, ncw = 0;
       int base = js;
-      for (int t = 0; t < full; t++, base += 16) {
-        zw += tiled_tile<P, 16, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+      for (int t = 0; t < full; t++, base += MT) {
+        zw += tiled_tile<P, MT, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
         cw = ncw << (32 - cols);  // column 0's carry at bit 31
         ncw = 0;
       }
-      for (; rem >= 16; rem -= 16, base += 16) {
-        zw += tiled_tile<P, 16, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+      for (; rem >= MT; rem -= MT, base += MT) {
+        zw += tiled_tile<P, MT, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
         cw = ncw << (32 - cols);
         ncw = 0;
       }
-      if (rem > 0) zw += tiled_rem<P, RING>(rem, ring, s_pl, base, je, cols, cur, cw, ncw);
+      if (rem > 0) zw += tiled_rem<P, RING, MT>(rem, ring, s_pl, base, je, cols, cur, cw, ncw);
     }
     i++;
     bool finished = i >= nq;

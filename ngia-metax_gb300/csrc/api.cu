@@ -52,8 +52,8 @@ int pull_state(ngia_ctx *c) {
 // batch members keep them on one stream (the batch runs jobs side by side).
 int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond) {
   const bool prof = c->profiling && !graph;
-  if (prof) CK(cudaEventRecord(c->ev_p0, c->stream));
   CK(ngia::launch_prep(c, -1));
+  if (prof) CK(cudaEventRecord(c->ev_p0, c->stream));
   CK(ngia::launch_filter(c));
   if (prof) CK(cudaEventRecord(c->ev_p1, c->stream));
   const int nc = ngia::num_classes(c->db.type);
@@ -252,7 +252,7 @@ int ngia::drv::open_ctx(const ngia_db_view *v, bool batch_member, ngia_ctx **out
   if (!ok) return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation of run buffers failed"));
   cudaMemsetAsync(rb.rep_list, 0, 4 * ngia::kListWords, c->stream);
   // launch shapes
-  if (ngia::align_configure(type, c->db.max_nb) != cudaSuccess)
+  if (ngia::align_configure(type, c->db.max_nb) != cudaSuccess || ngia::filter_configure() != cudaSuccess)
     return bail(fail(NGIA_E_CUDA, "ngia_open: kernel attributes"));
   for (int k = 0; k < ngia::num_classes(type); k++)
     c->grid_align[k] = c->num_sms * ngia::align_occupancy(type, k, c->db.max_nb);

@@ -86,6 +86,15 @@ struct RunParams {
   int32_t refill;         // tiled alignment: idle lanes a warp waits for before it claims new pairs
 };
 
+// Order of the two cheap-to-expensive tests.  Both orders give the same
+// members (a candidate joins iff all three tests pass); the short-word filter
+// goes first when it is expected to reject most candidates.
+__host__ __device__ inline int word_first_of(int type, const RunParams &prm) {
+  if (prm.word_order == 1) return 1;
+  if (prm.word_order == 2) return 0;
+  return type == 0 ? (prm.s >= 0.93f) : 1;
+}
+
 // Device buffers of one clustering run.
 struct RunBufs {
   RunState *st;

@@ -64,4 +64,5 @@ cudaError_t launch_align(ngia_ctx *c, int cls, cudaStream_t s, int score_mode);
 int align_occupancy(int type, int cls, int max_nb);
 int align_threads();
 cudaError_t align_configure(int type, int max_nb);
+cudaError_t filter_configure();
 }  // namespace ngia

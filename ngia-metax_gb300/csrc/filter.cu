@@ -10,6 +10,7 @@
 //                   updateJobs (305-320)
 //   k_next          updateRepresent assignment/selection (190-215): the next
 //                   representative is the first unclustered sequence
+#include <algorithm>
 #include <climits>
 
 #include "ctx.h"
@@ -78,14 +79,7 @@ __global__ void k_init_run(DevDB db, RunBufs rb, RunParams prm) {
     st->iter = 0;
     st->iter_limit = LLONG_MAX;
     for (int k = 0; k < kNumClasses; k++) st->qcount[k] = st->qhead[k] = 0;
-    // Order of the two cheap-to-expensive tests.  Both orders give the same
-    // members (a candidate joins iff all three tests pass); the short-word
-    // filter goes first when it is expected to reject most candidates.
-    int wf;
-    if (prm.word_order == 1) wf = 1;
-    else if (prm.word_order == 2) wf = 0;
-    else wf = db.type == 0 ? (prm.s >= 0.93f) : 1;
-    st->word_first = wf;
+    st->word_first = word_first_of(db.type, prm);
     st->word_active = 0;
     st->rep_nb = st->rep_len = st->rep_net = 0;
     st->st_candidates = st->st_base_pass = st->st_align_pairs = st->st_members = 0;
@@ -200,6 +194,200 @@ __device__ int word_count(const uint32_t *__restrict__ planes, int net2, int w, 
   return sum;
 }
 
+// ---- fast short-word count (filter stage) --------------------------------------
+// The filter looks words up in a byte table (tab[word] = 1 if the
+// representative holds the word), expanded in shared memory from the k-mer
+// bitset.  Positions q < w-1 have no full word (func.cu:376-396 counts from
+// position w-1): the loops below count every position with a zero-filled
+// history and then subtract those first w-1 lookups, recomputed the same way.
+
+// Spreads the 16 low bits of x onto the even bits of a 32-bit word.
+__device__ __forceinline__ uint32_t spread16(uint32_t x) {
+  x = (x | (x << 8)) & 0x00FF00FFu;
+  x = (x | (x << 4)) & 0x0F0F0F0Fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+// 2-bit code stream of one 32-residue DNA block as a 64-bit value (hi:lo),
+// earliest residue in the highest bits: residue j's code at bits 2(31-j)
+// (plane 0) and 2(31-j)+1 (plane 1).  With the previous block's low word
+// above it, the word ending at residue j is the low 2w bits of
+// (prev_lo:hi:lo) >> 2(31-j): one funnel shift and one mask.
+__device__ __forceinline__ void dna_stream(uint32_t p0, uint32_t p1, uint32_t &hi, uint32_t &lo) {
+  const uint32_t r0 = __brev(p0), r1 = __brev(p1);
+  hi = spread16(r0 >> 16) | (spread16(r1 >> 16) << 1);
+  lo = spread16(r0 & 0xFFFFu) | (spread16(r1 & 0xFFFFu) << 1);
+}
+
+// Occurrences of DNA block words in the table: all 32 positions (full) or
+// the first lim positions.
+__device__ __forceinline__ int dna_block_full(uint32_t prev, uint32_t hi, uint32_t lo, uint32_t mask,
+                                              const uint8_t *tab) {
+  int sum = 0;
+#pragma unroll
+  for (int j = 0; j < 16; j++) sum += tab[__funnelshift_r(hi, prev, 30 - 2 * j) & mask];
+#pragma unroll
+  for (int j = 16; j < 32; j++) sum += tab[__funnelshift_r(lo, hi, 62 - 2 * j) & mask];
+  return sum;
+}
+
+__device__ __forceinline__ uint32_t dna_word_at(uint32_t prev, uint32_t hi, uint32_t lo, int j) {
+  const int sh = 62 - 2 * j;
+  return sh >= 32 ? __funnelshift_r(hi, prev, sh - 32) : __funnelshift_r(lo, hi, sh);
+}
+
+__device__ __forceinline__ int dna_block_part(uint32_t prev, uint32_t hi, uint32_t lo, int lim, uint32_t mask,
+                                              const uint8_t *tab) {
+  int sum = 0;
+  for (int j = 0; j < lim; j++) sum += tab[dna_word_at(prev, hi, lo, j) & mask];
+  return sum;
+}
+
+// First w-1 positions of DNA block 0 (zero-filled history), to subtract.
+__device__ __forceinline__ int dna_head(const uint32_t *planes, int net2, int w, uint32_t mask, const uint8_t *tab) {
+  const int head = min(w - 1, net2);
+  if (head <= 0) return 0;
+  uint32_t hi, lo;
+  dna_stream(__ldg(planes), __ldg(planes + 1), hi, lo);
+  int sum = 0;
+  for (int j = 0; j < head; j++) sum += tab[dna_word_at(0u, hi, lo, j) & mask];
+  return sum;
+}
+
+// Code of residue j of a block (P planes).
+template <int P>
+__device__ __forceinline__ uint32_t code_of(const uint32_t (&pl)[P], int j) {
+  uint32_t c = 0;
+#pragma unroll
+  for (int p = 0; p < P; p++) c |= ((pl[p] >> j) & 1u) << p;
+  return c;
+}
+
+// Protein: rolling word over the residues of one block.
+template <int P>
+__device__ __forceinline__ int roll_block(const uint32_t (&pl)[P], int lim, uint32_t &word, uint32_t mask,
+                                          const uint8_t *tab) {
+  constexpr int bits = P == 2 ? 2 : 5;
+  int sum = 0;
+  if (lim == 32) {
+#pragma unroll
+    for (int j = 0; j < 32; j++) {
+      word = ((word << bits) | code_of<P>(pl, j)) & mask;
+      sum += tab[word];
+    }
+  } else {
+    for (int j = 0; j < lim; j++) {
+      word = ((word << bits) | code_of<P>(pl, j)) & mask;
+      sum += tab[word];
+    }
+  }
+  return sum;
+}
+
+template <int P>
+__device__ __forceinline__ int roll_head(const uint32_t *planes, int net2, int w, uint32_t mask, const uint8_t *tab) {
+  constexpr int bits = P == 2 ? 2 : 5;
+  const int head = min(w - 1, net2);
+  if (head <= 0) return 0;
+  uint32_t pl[P];
+#pragma unroll
+  for (int p = 0; p < P; p++) pl[p] = __ldg(planes + p);
+  uint32_t word = 0;
+  int sum = 0;
+  for (int j = 0; j < head; j++) {
+    word = ((word << bits) | code_of<P>(pl, j)) & mask;
+    sum += tab[word];
+  }
+  return sum;
+}
+
+// Short-word count of one candidate by one thread.
+template <int P>
+__device__ int word_count_fast(const uint32_t *__restrict__ planes, int net2, int w, const uint8_t *tab) {
+  constexpr int bits = P == 2 ? 2 : 5;
+  const uint32_t mask = (1u << (w * bits)) - 1u;
+  const int nfull = net2 >> 5, rest = net2 & 31;
+  int sum = 0;
+  if (P == 2) {
+    uint32_t prev = 0, hi, lo;
+    for (int b = 0; b < nfull; b++) {
+      dna_stream(__ldg(planes + 2 * b), __ldg(planes + 2 * b + 1), hi, lo);
+      sum += dna_block_full(prev, hi, lo, mask, tab);
+      prev = lo;
+    }
+    if (rest) {
+      dna_stream(__ldg(planes + 2 * nfull), __ldg(planes + 2 * nfull + 1), hi, lo);
+      sum += dna_block_part(prev, hi, lo, rest, mask, tab);
+    }
+    return sum - dna_head(planes, net2, w, mask, tab);
+  } else {
+    uint32_t word = 0;
+    for (int b = 0; b <= nfull; b++) {
+      const int lim = b < nfull ? 32 : rest;
+      if (!lim) break;
+      uint32_t pl[P];
+#pragma unroll
+      for (int p = 0; p < P; p++) pl[p] = __ldg(planes + b * P + p);
+      sum += roll_block<P>(pl, lim, word, mask, tab);
+    }
+    return sum - roll_head<P>(planes, net2, w, mask, tab);
+  }
+}
+
+// Short-word count of one candidate by the whole warp: lane l takes blocks
+// l, l+32, ...; each lane's history (the previous block) comes from the lane
+// below by a shuffle.  All 32 lanes call it with the same arguments.
+template <int P>
+__device__ int word_count_warp(const uint32_t *__restrict__ planes, int net2, int w, const uint8_t *tab) {
+  constexpr int bits = P == 2 ? 2 : 5;
+  const uint32_t mask = (1u << (w * bits)) - 1u;
+  const int lane = threadIdx.x & 31;
+  const int nb = (net2 + 31) >> 5;
+  int sum = 0;
+  uint32_t carry[P];  // planes (DNA: the stream's low word) of the block below lane 0's
+#pragma unroll
+  for (int p = 0; p < P; p++) carry[p] = 0u;
+  for (int b0 = 0; b0 < nb; b0 += 32) {
+    const int b = b0 + lane;
+    const bool have = b < nb;
+    const int lim = have ? min(32, net2 - 32 * b) : 0;
+    uint32_t pl[P];
+#pragma unroll
+    for (int p = 0; p < P; p++) pl[p] = have ? __ldg(planes + b * P + p) : 0u;
+    if (P == 2) {
+      uint32_t hi, lo;
+      dna_stream(pl[0], pl[1], hi, lo);
+      uint32_t prev = __shfl_up_sync(kFullMask, lo, 1);
+      if (lane == 0) prev = carry[0];
+      if (lim == 32) sum += dna_block_full(prev, hi, lo, mask, tab);
+      else if (lim > 0) sum += dna_block_part(prev, hi, lo, lim, mask, tab);
+      carry[0] = __shfl_sync(kFullMask, lo, 31);
+    } else {
+      uint32_t pv[P];
+#pragma unroll
+      for (int p = 0; p < P; p++) {
+        pv[p] = __shfl_up_sync(kFullMask, pl[p], 1);
+        if (lane == 0) pv[p] = carry[p];
+      }
+      // history: the last w-1 residues of the block below
+      uint32_t word = 0;
+      for (int j = 32 - (w - 1); j < 32; j++) word = ((word << bits) | code_of<P>(pv, j)) & mask;
+      if (lim > 0) sum += roll_block<P>(pl, lim, word, mask, tab);
+#pragma unroll
+      for (int p = 0; p < P; p++) carry[p] = __shfl_sync(kFullMask, pl[p], 31);
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFullMask, sum, o);
+  if (P == 2) return sum - dna_head(planes, net2, w, mask, tab);
+  return sum - roll_head<P>(planes, net2, w, mask, tab);
+}
+
+// Candidates longer than this are counted by the whole warp.
+constexpr int kWarpWordLen = 2048;
+
 // Composition sum of candidate c against the representative counts rc[].
 template <int A>
 __device__ __forceinline__ int base_sum(const uint32_t *__restrict__ cnt, int c, const uint32_t *rc) {
@@ -251,12 +439,20 @@ __device__ __forceinline__ void flush_stats(RunState *st, unsigned long long can
   }
 }
 
-// Fused filter over the unclustered set.  One warp per 32-sequence bitmap
-// word: lanes read the header arrays of 32 consecutive sequences (coalesced),
-// apply the composition test and, in word-first order, the short-word test
-// (shared-memory k-mer bitset), then compact survivors into the alignment
-// class queues.  `exact` = 1 runs the composition stage only and records the
-// survivors (bitmap in rb.flags) for the exact short-word path.
+// Fused filter over the unclustered set, one tile of kFilterTileWords
+// bitmap words (1,024 sequences) per CTA pass: each warp takes
+// kFilterWordsPerWarp consecutive words; lanes read the header arrays of 32
+// consecutive sequences (coalesced), apply the composition test and, in
+// word-first order, the short-word test (shared-memory k-mer bitset).
+// Survivors are compacted into the alignment class queues in two levels:
+// warp-aggregated shared-memory counters give each survivor its slot inside
+// the tile, then one global atomic per class and tile reserves the tile's
+// range, so the global queue counters see ~1/1,000 of the candidates.
+// `exact` = 1 runs the composition stage only and records the survivors
+// (bitmap in rb.flags) for the exact short-word path.
+constexpr int kFilterWordsPerWarp = 4;
+constexpr int kFilterTileWords = 8 * kFilterWordsPerWarp;  // 256 threads
+
 template <int P>
 __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams prm, int exact) {
   RunState *st = rb.st;
@@ -264,6 +460,7 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
   __shared__ uint64_t bar;
   __shared__ uint32_t s_rc[28];
   __shared__ int s_hdr[4];
+  __shared__ uint32_t s_cnt[kNumClasses], s_base[kNumClasses];
   constexpr int A = P == 2 ? 4 : 28;
   if (threadIdx.x == 0) {
     const bool skip = st->done || st->iter >= st->iter_limit || st->err;
@@ -277,47 +474,103 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
   if (s_hdr[0]) return;
   const int L1 = s_hdr[1], nb1 = s_hdr[2], word_here = s_hdr[3];
   const int list_words = max(1, (int)((1u << (prm.w * (P == 2 ? 2 : 5))) / 32u));
+  // byte table of the k-mer bitset, right after the bitset
+  uint8_t *s_tab = reinterpret_cast<uint8_t *>(s_list + list_words);
   if (word_here) {
     if (!stage_to_smem(s_list, rb.rep_list, (uint32_t)list_words, &bar, st, 1)) return;
+    for (int i = threadIdx.x; i < list_words * 8; i += blockDim.x) {
+      const uint32_t nib = (s_list[i >> 3] >> (4 * (i & 7))) & 0xFu;  // 4 words -> 4 bytes
+      reinterpret_cast<uint32_t *>(s_tab)[i] = (nib & 1u) | ((nib & 2u) << 7) | ((nib & 4u) << 14) | ((nib & 8u) << 21);
+    }
+    __syncthreads();
   }
   const float s = prm.s;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nbw = (db.n + 31) / 32;
-  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int tiles = (nbw + kFilterTileWords - 1) / kFilterTileWords;
+  // Bitmap word of slot k of a tile.  With the short-word test here, a
+  // tile's words are spread over the (length-sorted) database so that every
+  // tile holds a share of the long candidates; otherwise they are
+  // consecutive, which keeps neighbouring queue entries of similar length.
+  auto word_of = [&](int tile, int k) {
+    return word_here ? k * tiles + tile : tile * kFilterTileWords + k;
+  };
   unsigned long long cand = 0, base = 0, bytes = 0, wchk = 0, wpass = 0;
-  for (int wi = gw; wi < nbw; wi += nwarps) {
-    const uint32_t bits = rb.alive[wi];
-    if (!bits) {
-      if (exact && lane == 0) reinterpret_cast<uint32_t *>(rb.flags)[wi] = 0;
-      continue;
-    }
-    const int c = wi * 32 + lane;
-    const bool alive = (bits >> lane) & 1u;
-    bool pass = false;
-    int cls = 0;
-    if (alive) {
-      cand++;
-      bytes += 4 * (2 + A);
-      const int L2 = __ldg(db.len + c);
-      pass = !(base_sum<A>(db.cnt, c, s_rc) < cutoff_of(L2, s));
-      if (pass) base++;
-      if (pass && word_here) {
-        const int net2 = __ldg(db.net + c);
-        const uint32_t *planes = db.words + __ldg(db.off + c) + db.hw;
-        const int ws = word_count<P>(planes, net2, prm.w, s_list);
-        wchk++;
-        bytes += 4ull * P * ((net2 + 31) / 32);
-        pass = !(ws < word_min(L2, prm.w, s));
-        if (pass) wpass++;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    if (threadIdx.x < kNumClasses) s_cnt[threadIdx.x] = 0;
+    __syncthreads();
+    int slot[kFilterWordsPerWarp], cls_of[kFilterWordsPerWarp];
+#pragma unroll
+    for (int k = 0; k < kFilterWordsPerWarp; k++) {
+      slot[k] = -1;
+      cls_of[k] = 0;
+      const int wi = word_of(tile, warp * kFilterWordsPerWarp + k);
+      if (wi >= nbw) continue;  // warp-uniform
+      const uint32_t bits = rb.alive[wi];
+      if (!bits) {
+        if (exact && lane == 0) reinterpret_cast<uint32_t *>(rb.flags)[wi] = 0;
+        continue;
       }
-      if (pass && !exact) cls = class_of(db.type, window_of(band_blocks(L1, L2, s), nb1));
+      const int c = wi * 32 + lane;
+      const bool alive = (bits >> lane) & 1u;
+      bool pass = false, deferred = false;
+      int cls = 0;
+      if (alive) {
+        cand++;
+        bytes += 4 * (2 + A);
+        const int L2 = __ldg(db.len + c);
+        pass = !(base_sum<A>(db.cnt, c, s_rc) < cutoff_of(L2, s));
+        if (pass) base++;
+        if (pass && word_here) {
+          const int net2 = __ldg(db.net + c);
+          wchk++;
+          bytes += 4ull * P * ((net2 + 31) / 32);
+          if (net2 <= kWarpWordLen) {
+            const uint32_t *planes = db.words + __ldg(db.off + c) + db.hw;
+            pass = !(word_count_fast<P>(planes, net2, prm.w, s_tab) < word_min(L2, prm.w, s));
+            if (pass) wpass++;
+          } else {
+            deferred = true;
+          }
+        }
+      }
+      // long candidates: the whole warp counts each one
+      for (unsigned dm = __ballot_sync(kFullMask, deferred); dm; dm &= dm - 1) {
+        const int src = __ffs(dm) - 1;
+        const int cc = wi * 32 + src;
+        const uint32_t *planes = db.words + __ldg(db.off + cc) + db.hw;
+        const int ws = word_count_warp<P>(planes, __ldg(db.net + cc), prm.w, s_tab);
+        if (lane == src) {
+          pass = !(ws < word_min(__ldg(db.len + cc), prm.w, s));
+          if (pass) wpass++;
+        }
+      }
+      if (alive && pass && !exact) cls = class_of(db.type, window_of(band_blocks(L1, __ldg(db.len + c), s), nb1));
+      const unsigned pm = __ballot_sync(kFullMask, pass);
+      if (exact) {
+        if (lane == 0) reinterpret_cast<uint32_t *>(rb.flags)[wi] = pm;
+        continue;
+      }
+      if (pass) {
+        const unsigned peers = __match_any_sync(pm, cls);
+        const int leader = __ffs(peers) - 1;
+        uint32_t b = 0;
+        if (lane == leader) b = atomicAdd(&s_cnt[cls], (uint32_t)__popc(peers));
+        b = __shfl_sync(peers, b, leader);
+        slot[k] = (int)(b + __popc(peers & ((1u << lane) - 1u)));
+        cls_of[k] = cls;
+      }
     }
-    if (exact) {
-      const unsigned m = __ballot_sync(kFullMask, pass);
-      if (lane == 0) reinterpret_cast<uint32_t *>(rb.flags)[wi] = m;
-    } else {
-      push_queue(rb, st, pass, cls, c);
+    __syncthreads();
+    if (threadIdx.x < kNumClasses)
+      s_base[threadIdx.x] = s_cnt[threadIdx.x] ? atomicAdd(&st->qcount[threadIdx.x], s_cnt[threadIdx.x]) : 0u;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < kFilterWordsPerWarp; k++) {
+      if (slot[k] >= 0) {
+        const int c = word_of(tile, warp * kFilterWordsPerWarp + k) * 32 + lane;
+        rb.queue[cls_of[k]][s_base[cls_of[k]] + (uint32_t)slot[k]] = c;
+      }
     }
   }
   flush_stats(st, cand, base, bytes, wchk, wpass);
@@ -420,6 +673,15 @@ __global__ void __launch_bounds__(256) k_word_exact(DevDB db, RunBufs rb, RunPar
   flush_stats(st, 0, 0, bytes, wchk, wpass);
 }
 
+// Largest filter shared memory: DNA w=8 bitset (8 KB) + byte table (64 KB).
+cudaError_t filter_configure() {
+  const int most = 9 * (1 << 16) / 8;
+  cudaError_t e = cudaFuncSetAttribute((const void *)k_filter<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute((const void *)k_filter<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+  return e;
+}
+
 cudaError_t launch_filter(ngia_ctx *c) {
   const int P = c->db.P;
   const int bits = c->db.type ? 5 : 2;
@@ -428,18 +690,21 @@ cudaError_t launch_filter(ngia_ctx *c) {
   // Exact path only matters when the short-word filter can run and some
   // record is shorter than 16 residues.
   const bool exact = c->db.has_short && !c->prm.precise;
+  const int nbw = (c->db.n + 31) / 32;
+  const int grid = std::max(1, std::min(c->grid_filter, (nbw + kFilterTileWords - 1) / kFilterTileWords));
   if (!exact) {
+    // word-first order also holds the byte table (8 bytes per bitset byte)
+    const size_t fsmem = word_first_of(c->db.type, c->prm) ? smem * 9 : smem;
     if (P == 2)
-      k_filter<2><<<c->grid_filter, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
+      k_filter<2><<<grid, 256, fsmem, c->stream>>>(c->db, c->rb, c->prm, 0);
     else
-      k_filter<5><<<c->grid_filter, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
+      k_filter<5><<<grid, 256, fsmem, c->stream>>>(c->db, c->rb, c->prm, 0);
     return cudaGetLastError();
   }
   if (P == 2)
-    k_filter<2><<<c->grid_filter, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
+    k_filter<2><<<grid, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
   else
-    k_filter<5><<<c->grid_filter, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
-  const int nbw = (c->db.n + 31) / 32;
+    k_filter<5><<<grid, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
   k_scan_words<<<1, 1024, 0, c->stream>>>(reinterpret_cast<const uint32_t *>(c->rb.flags), nbw, c->rb.scan_part);
   k_first_short<<<64, 256, 0, c->stream>>>(c->db, c->rb, 1);
   k_first_short<<<c->num_sms * 2, 256, 0, c->stream>>>(c->db, c->rb, 0);

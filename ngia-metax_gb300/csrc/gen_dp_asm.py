@@ -16,7 +16,7 @@ Run `python gen_dp_asm.py` after editing; the output is committed.
 from pathlib import Path
 
 PLANES = (2, 5)
-WIDTHS = tuple(range(1, 17)) + (24, 32)
+WIDTHS = tuple(range(1, 33))
 
 
 def one(P: int, TW: int, cin: bool, cout: bool) -> str:

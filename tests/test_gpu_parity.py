@@ -113,6 +113,21 @@ def test_cluster_protein(cuda_device, s, w):
     _check_cluster(db, ngia.params_clamp(1, s, w, 0))
 
 
+@pytest.mark.parametrize("db_type,s,w", [(0, 0.95, 5), (0, 0.93, 8), (1, 0.9, 3), (1, 0.5, 2)])
+def test_cluster_long_records_word_first(cuda_device, db_type, s, w):
+    """Short-word test first, on candidates both sides of 2,048 residues:
+    the filter counts the longer ones with the whole warp."""
+    if db_type == 0:
+        db = family_db(0, n=160, anc=6, seed=61, len_a=2100.0, len_b=500.0, len_min=1200, len_max=6000,
+                       subst_max=0.05)
+    else:
+        db = family_db(1, n=160, anc=6, seed=62, len_a=2000.0, len_b=0.6, len_min=200, len_max=9000,
+                       subst_max=0.15)
+    net = db.words[db.rec_off + 1]
+    assert (net > 2048).sum() >= 20 and (net <= 2048).sum() >= 20
+    _check_cluster(db, ngia.params_clamp(db_type, s, w, 0))
+
+
 @pytest.mark.parametrize("order", ["1", "2"])
 def test_word_orders_agree(cuda_device, order, monkeypatch):
     """Short-word test before or after the alignment: same members."""
