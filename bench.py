@@ -162,14 +162,19 @@ def make_db(args):
     return db, cfg
 
 
-def workload_desc(args, cfg) -> dict:
-    return {"workload": f"{args.workload}: {cfg['n_seqs']:,} {'DNA' if cfg['type'] == 0 else 'protein'} "
-                        f"sequences, {cfg['n_ancestors']:,} ancestors, lengths ~N({cfg['len_a']:.0f},"
-                        f"{cfg['len_b']:.0f}) clipped [{cfg['len_min']},{cfg['len_max']}], s={args.similarity},"
-                        f" w={args.word}",
-            "iters_per_step": args.iters_per_step, "similarity": args.similarity, "word_length": args.word,
-            "driver": args.mode, "seed": args.seed,
-            "l2": "inputs larger than L2 (database 390 MB vs 129 MB L2)"}
+def workload_desc(args, cfg, db_bytes: int | None = None) -> dict:
+    dist = (f"~N({cfg['len_a']:.0f},{cfg['len_b']:.0f})" if cfg.get("len_dist", 0) == 0 else
+            f"log-normal(median {cfg['len_a']:.0f}, sigma {cfg['len_b']:g})")
+    out = {"workload": f"{args.workload}: {cfg['n_seqs']:,} {'DNA' if cfg['type'] == 0 else 'protein'} "
+                       f"sequences, {cfg['n_ancestors']:,} ancestors, lengths {dist} clipped "
+                       f"[{cfg['len_min']},{cfg['len_max']}], s={args.similarity}, w={args.word}",
+           "iters_per_step": args.iters_per_step, "similarity": args.similarity, "word_length": args.word,
+           "driver": args.mode, "seed": args.seed}
+    if db_bytes is not None:
+        big = db_bytes > 129e6
+        out["l2"] = (f"inputs {'larger' if big else 'smaller'} than L2 (database {db_bytes / 1e6:.0f} MB vs "
+                     f"129 MB L2)")
+    return out
 
 
 # ---- reference arm: the oracle on the host cores ---------------------------------
@@ -197,9 +202,9 @@ def run_reference(args, dist: Dist):
            "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "impl": "reference",
            "data": "synthetic (seeded generator with the configuration's shapes)",
-           "config": {**workload_desc(args, cfg), "iters_per_step": 1},
+           "config": {**workload_desc(args, cfg, db.words.nbytes), "iters_per_step": 1},
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": "first greedy iteration (representative vs all 1M sequences) per step"},
+                            "sample": f"first greedy iteration (representative vs all {db.n:,} sequences) per step"},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
 
@@ -257,7 +262,9 @@ def run_ours(args, dist: Dist):
 
     out = None
     if dist.rank == 0:
-        peak_gcell = int_gops * 32.0 / 4.0  # 4 INT32 operations per 32-cell word step (DNA)
+        planes = 2 if cfg["type"] == 0 else 5
+        ops = planes + 2  # INT32 operations per 32-cell word step: one LOP3 per plane, add, LOP3
+        peak_gcell = int_gops * 32.0 / ops
         peaks = measured_peaks()
         e2e = None
         if not args.skip_e2e:
@@ -269,7 +276,7 @@ def run_ours(args, dist: Dist):
                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
                "data": "synthetic (seeded generator with the configuration's shapes)",
-               "config": workload_desc(args, cfg),
+               "config": workload_desc(args, cfg, db.words.nbytes),
                "gcups": total_cells / T / 1e9,
                "gcups_note": "reference band cells (func.cu loop bounds) of the pairs aligned, per second",
                "wall_s_timed": t_wall,
@@ -277,7 +284,7 @@ def run_ours(args, dist: Dist):
                             "achieved": done_gcell, "peak": peak_gcell, "unit": "Gcell/s",
                             "frac": done_gcell / peak_gcell if peak_gcell else None, "traffic": None,
                             "peak_source": f"of measured INT32 issue rate {int_gops:.0f} Gop/s (probe) x 32 cells"
-                                           f" / 4 ops", "reference_cells_rate": band_gcell,
+                                           f" / {ops} ops", "reference_cells_rate": band_gcell,
                             "profiled_iterations": prof_iters, "ms_align_per_iter": ms_align / prof_iters,
                             "class_ms_per_iter": [round((y - x) / prof_iters, 3) for x, y in
                                                   zip(a["class_ms"], b["class_ms"])],

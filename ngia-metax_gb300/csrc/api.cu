@@ -248,9 +248,11 @@ int ngia::drv::open_ctx(const ngia_db_view *v, bool batch_member, ngia_ctx **out
             dalloc(&rb.first_short, ngia::kRefGridThreads) == cudaSuccess &&
             dalloc(&rb.scan_part, nbw) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&rb.flags, 4 * std::max<size_t>(nbw, 1)) == cudaSuccess;
+  ok = ok && dalloc(&rb.fstats, (size_t)ngia::kFilterStripes * ngia::kFilterStats) == cudaSuccess;
   for (int k = 0; ok && k < ngia::num_classes(type); k++) ok = dalloc(&rb.queue[k], (size_t)n) == cudaSuccess;
   if (!ok) return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation of run buffers failed"));
   cudaMemsetAsync(rb.rep_list, 0, 4 * ngia::kListWords, c->stream);
+  cudaMemsetAsync(rb.fstats, 0, 8 * ngia::kFilterStripes * ngia::kFilterStats, c->stream);
   // launch shapes
   if (ngia::align_configure(type, c->db.max_nb) != cudaSuccess || ngia::filter_configure() != cudaSuccess)
     return bail(fail(NGIA_E_CUDA, "ngia_open: kernel attributes"));
@@ -298,6 +300,7 @@ extern "C" int ngia_close(ngia_ctx *c) {
   cudaFree(rb.first_short);
   cudaFree(rb.scan_part);
   cudaFree(rb.flags);
+  cudaFree(rb.fstats);
   cudaFree(rb.scratch);
   for (int k = 0; k < ngia::kNumClasses; k++) cudaFree(rb.queue[k]);
   if (c->h_state) cudaFreeHost(c->h_state);

@@ -112,10 +112,16 @@ struct RunBufs {
   uint32_t *scratch;      // per-lane line storage of the generic kernel
   int64_t scratch_words;
   int32_t generic_lanes;
+  // filter counters, 32 stripes x kFilterStats (one 64-byte line each),
+  // added per CTA and folded into the run state by k_next
+  unsigned long long *fstats;
   // pair-score mode
   const int32_t *score_cands;
   int32_t *score_out;
 };
+
+constexpr int kFilterStats = 8;     // counters per stripe (5 used)
+constexpr int kFilterStripes = 32;
 
 #define NGIA_ERR_MBAR_TIMEOUT 1
 #define NGIA_ERR_SCRATCH 2

@@ -85,6 +85,7 @@ __global__ void k_init_run(DevDB db, RunBufs rb, RunParams prm) {
     st->st_candidates = st->st_base_pass = st->st_align_pairs = st->st_members = 0;
     st->st_band_cells = st->st_filter_bytes = st->st_word_checks = st->st_word_pass = 0;
     st->st_done_cells = 0;
+    for (int k = 0; k < kFilterStripes * kFilterStats; k++) rb.fstats[k] = 0;
     for (int k = 0; k < kNumClasses; k++) st->st_class_pairs[k] = 0;
   }
 }
@@ -420,9 +421,16 @@ __device__ __forceinline__ void push_queue(RunBufs &rb, RunState *st, bool pass,
   rb.queue[cls][base + __popc(peers & ((1u << lane) - 1u))] = c;
 }
 
-__device__ __forceinline__ void flush_stats(RunState *st, unsigned long long cand, unsigned long long base,
+// Adds the filter counters of the calling CTA (every thread calls it) to one
+// of kFilterStripes counter stripes; k_next folds the stripes into the run
+// state.  One warp-level and one CTA-level reduction keep the global atomics
+// at five per CTA, spread over 32 cache lines.
+__device__ __forceinline__ void flush_stats(const RunBufs &rb, unsigned long long cand, unsigned long long base,
                                             unsigned long long bytes, unsigned long long wchk,
                                             unsigned long long wpass) {
+  __shared__ unsigned long long s_acc[5];
+  if (threadIdx.x < 5) s_acc[threadIdx.x] = 0;
+  __syncthreads();
   for (int o = 16; o; o >>= 1) {
     cand += __shfl_down_sync(kFullMask, cand, o);
     base += __shfl_down_sync(kFullMask, base, o);
@@ -431,16 +439,19 @@ __device__ __forceinline__ void flush_stats(RunState *st, unsigned long long can
     wpass += __shfl_down_sync(kFullMask, wpass, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    if (cand) atomicAdd(&st->st_candidates, cand);
-    if (base) atomicAdd(&st->st_base_pass, base);
-    if (bytes) atomicAdd(&st->st_filter_bytes, bytes);
-    if (wchk) atomicAdd(&st->st_word_checks, wchk);
-    if (wpass) atomicAdd(&st->st_word_pass, wpass);
+    if (cand) atomicAdd(&s_acc[0], cand);
+    if (base) atomicAdd(&s_acc[1], base);
+    if (bytes) atomicAdd(&s_acc[2], bytes);
+    if (wchk) atomicAdd(&s_acc[3], wchk);
+    if (wpass) atomicAdd(&s_acc[4], wpass);
   }
+  __syncthreads();
+  if (threadIdx.x < 5 && s_acc[threadIdx.x])
+    atomicAdd(&rb.fstats[(blockIdx.x % kFilterStripes) * kFilterStats + threadIdx.x], s_acc[threadIdx.x]);
 }
 
 // Fused filter over the unclustered set, one tile of kFilterTileWords
-// bitmap words (1,024 sequences) per CTA pass: each warp takes
+// bitmap words (8 warps x kFilterWordsPerWarp words) per CTA pass: each warp takes
 // kFilterWordsPerWarp consecutive words; lanes read the header arrays of 32
 // consecutive sequences (coalesced), apply the composition test and, in
 // word-first order, the short-word test (shared-memory k-mer bitset).
@@ -450,11 +461,21 @@ __device__ __forceinline__ void flush_stats(RunState *st, unsigned long long can
 // range, so the global queue counters see ~1/1,000 of the candidates.
 // `exact` = 1 runs the composition stage only and records the survivors
 // (bitmap in rb.flags) for the exact short-word path.
-constexpr int kFilterWordsPerWarp = 4;
-constexpr int kFilterTileWords = 8 * kFilterWordsPerWarp;  // 256 threads
+// Bitmap words per warp and tile pass.  Swept on GB300 (1M DNA s=0.85 and
+// 200k protein s=0.9): the composition test alone is fastest with 8 (fewer,
+// fuller CTAs: 20.7 us vs 23.1 us with 4), the short-word test in the filter
+// with 1 (protein 0.21 ms vs 0.24 / 0.37 / 0.61 ms with 2 / 4 / 8: more
+// tiles share the long candidates; DNA s=0.95 is the same for 1 to 4).
+#ifndef NGIA_FILTER_WPW_BASE
+#define NGIA_FILTER_WPW_BASE 8
+#endif
+#ifndef NGIA_FILTER_WPW_WORD
+#define NGIA_FILTER_WPW_WORD 1
+#endif
 
-template <int P>
+template <int P, int kFilterWordsPerWarp>
 __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams prm, int exact) {
+  constexpr int kFilterTileWords = 8 * kFilterWordsPerWarp;  // 256 threads
   RunState *st = rb.st;
   extern __shared__ __align__(16) uint32_t s_list[];
   __shared__ uint64_t bar;
@@ -499,22 +520,25 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     if (threadIdx.x < kNumClasses) s_cnt[threadIdx.x] = 0;
     __syncthreads();
+    // The warp's bitmap words first, then every header load of all its
+    // words (independent of one another), then the compaction.
     int slot[kFilterWordsPerWarp], cls_of[kFilterWordsPerWarp];
+    uint32_t bits_of[kFilterWordsPerWarp];
 #pragma unroll
     for (int k = 0; k < kFilterWordsPerWarp; k++) {
-      slot[k] = -1;
-      cls_of[k] = 0;
       const int wi = word_of(tile, warp * kFilterWordsPerWarp + k);
-      if (wi >= nbw) continue;  // warp-uniform
-      const uint32_t bits = rb.alive[wi];
-      if (!bits) {
-        if (exact && lane == 0) reinterpret_cast<uint32_t *>(rb.flags)[wi] = 0;
-        continue;
-      }
+      bits_of[k] = wi < nbw ? rb.alive[wi] : 0u;
+    }
+    unsigned pass_of = 0;  // bit k: this lane's candidate of word k survives
+#pragma unroll
+    for (int k = 0; k < kFilterWordsPerWarp; k++) {
+      cls_of[k] = 0;
+      const uint32_t bits = bits_of[k];
+      if (!bits) continue;  // warp-uniform
+      const int wi = word_of(tile, warp * kFilterWordsPerWarp + k);
       const int c = wi * 32 + lane;
       const bool alive = (bits >> lane) & 1u;
       bool pass = false, deferred = false;
-      int cls = 0;
       if (alive) {
         cand++;
         bytes += 4 * (2 + A);
@@ -533,6 +557,7 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
             deferred = true;
           }
         }
+        if (pass && !exact) cls_of[k] = class_of(db.type, window_of(band_blocks(L1, L2, s), nb1));
       }
       // long candidates: the whole warp counts each one
       for (unsigned dm = __ballot_sync(kFullMask, deferred); dm; dm &= dm - 1) {
@@ -541,24 +566,35 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
         const uint32_t *planes = db.words + __ldg(db.off + cc) + db.hw;
         const int ws = word_count_warp<P>(planes, __ldg(db.net + cc), prm.w, s_tab);
         if (lane == src) {
-          pass = !(ws < word_min(__ldg(db.len + cc), prm.w, s));
-          if (pass) wpass++;
+          const int L2 = __ldg(db.len + cc);
+          pass = !(ws < word_min(L2, prm.w, s));
+          if (pass) {
+            wpass++;
+            if (!exact) cls_of[k] = class_of(db.type, window_of(band_blocks(L1, L2, s), nb1));
+          }
         }
       }
-      if (alive && pass && !exact) cls = class_of(db.type, window_of(band_blocks(L1, __ldg(db.len + c), s), nb1));
+      if (pass) pass_of |= 1u << k;
+    }
+#pragma unroll
+    for (int k = 0; k < kFilterWordsPerWarp; k++) {
+      slot[k] = -1;
+      const int wi = word_of(tile, warp * kFilterWordsPerWarp + k);
+      if (wi >= nbw) continue;  // warp-uniform
+      const bool pass = (pass_of >> k) & 1u;
       const unsigned pm = __ballot_sync(kFullMask, pass);
       if (exact) {
         if (lane == 0) reinterpret_cast<uint32_t *>(rb.flags)[wi] = pm;
         continue;
       }
       if (pass) {
+        const int cls = cls_of[k];
         const unsigned peers = __match_any_sync(pm, cls);
         const int leader = __ffs(peers) - 1;
         uint32_t b = 0;
         if (lane == leader) b = atomicAdd(&s_cnt[cls], (uint32_t)__popc(peers));
         b = __shfl_sync(peers, b, leader);
         slot[k] = (int)(b + __popc(peers & ((1u << lane) - 1u)));
-        cls_of[k] = cls;
       }
     }
     __syncthreads();
@@ -573,7 +609,7 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
       }
     }
   }
-  flush_stats(st, cand, base, bytes, wchk, wpass);
+  flush_stats(rb, cand, base, bytes, wchk, wpass);
 }
 
 // ---- exact short-word path ---------------------------------------------------
@@ -670,16 +706,18 @@ __global__ void __launch_bounds__(256) k_word_exact(DevDB db, RunBufs rb, RunPar
     }
     push_queue(rb, st, pass, cls, c);
   }
-  flush_stats(st, 0, 0, bytes, wchk, wpass);
+  flush_stats(rb, 0, 0, bytes, wchk, wpass);
 }
 
 // Largest filter shared memory: DNA w=8 bitset (8 KB) + byte table (64 KB).
 cudaError_t filter_configure() {
   const int most = 9 * (1 << 16) / 8;
-  cudaError_t e = cudaFuncSetAttribute((const void *)k_filter<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute((const void *)k_filter<5>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
-  return e;
+  const void *fns[] = {(const void *)k_filter<2, NGIA_FILTER_WPW_WORD>, (const void *)k_filter<5, NGIA_FILTER_WPW_WORD>};
+  for (const void *f : fns) {
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_filter(ngia_ctx *c) {
@@ -691,20 +729,28 @@ cudaError_t launch_filter(ngia_ctx *c) {
   // record is shorter than 16 residues.
   const bool exact = c->db.has_short && !c->prm.precise;
   const int nbw = (c->db.n + 31) / 32;
-  const int grid = std::max(1, std::min(c->grid_filter, (nbw + kFilterTileWords - 1) / kFilterTileWords));
+  constexpr int kB = NGIA_FILTER_WPW_BASE, kW = NGIA_FILTER_WPW_WORD;
+  const int grid_b = std::max(1, std::min(c->grid_filter, (nbw + 8 * kB - 1) / (8 * kB)));
+  const int grid_w = std::max(1, std::min(c->grid_filter, (nbw + 8 * kW - 1) / (8 * kW)));
   if (!exact) {
     // word-first order also holds the byte table (8 bytes per bitset byte)
-    const size_t fsmem = word_first_of(c->db.type, c->prm) ? smem * 9 : smem;
-    if (P == 2)
-      k_filter<2><<<grid, 256, fsmem, c->stream>>>(c->db, c->rb, c->prm, 0);
-    else
-      k_filter<5><<<grid, 256, fsmem, c->stream>>>(c->db, c->rb, c->prm, 0);
+    if (word_first_of(c->db.type, c->prm)) {
+      if (P == 2)
+        k_filter<2, kW><<<grid_w, 256, smem * 9, c->stream>>>(c->db, c->rb, c->prm, 0);
+      else
+        k_filter<5, kW><<<grid_w, 256, smem * 9, c->stream>>>(c->db, c->rb, c->prm, 0);
+    } else {
+      if (P == 2)
+        k_filter<2, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
+      else
+        k_filter<5, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
+    }
     return cudaGetLastError();
   }
   if (P == 2)
-    k_filter<2><<<grid, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
+    k_filter<2, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
   else
-    k_filter<5><<<grid, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
+    k_filter<5, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
   k_scan_words<<<1, 1024, 0, c->stream>>>(reinterpret_cast<const uint32_t *>(c->rb.flags), nbw, c->rb.scan_part);
   k_first_short<<<64, 256, 0, c->stream>>>(c->db, c->rb, 1);
   k_first_short<<<c->num_sms * 2, 256, 0, c->stream>>>(c->db, c->rb, 0);
@@ -735,6 +781,17 @@ __global__ void k_next(DevDB db, RunBufs rb, unsigned long long cond, int use_co
   const int r = st->rep;
   const int nbw = (db.n + 31) / 32;
   if (threadIdx.x == 0) atomicAnd(&rb.alive[r >> 5], ~(1u << (r & 31)));
+  if (threadIdx.x < 5) {  // fold this iteration's filter counters
+    unsigned long long sum = 0;
+    for (int k = 0; k < kFilterStripes; k++) {
+      unsigned long long &f = rb.fstats[k * kFilterStats + threadIdx.x];
+      sum += f;
+      f = 0;
+    }
+    unsigned long long *dst[5] = {&st->st_candidates, &st->st_base_pass, &st->st_filter_bytes,
+                                  &st->st_word_checks, &st->st_word_pass};
+    *dst[threadIdx.x] += sum;
+  }
   __syncthreads();
   for (int base = r >> 5; base < nbw; base += blockDim.x) {
     const int wi = base + threadIdx.x;
