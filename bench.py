@@ -51,7 +51,9 @@ def parse():
     ap.add_argument("--iters-per-step", type=int, default=32)
     ap.add_argument("--similarity", type=float, default=0.85)
     ap.add_argument("--word", type=int, default=5)
-    ap.add_argument("--workload", default="dna_1m")
+    ap.add_argument("--workload", default="dna_1m", help="dna_small | dna_1m | protein_200k | batch256")
+    ap.add_argument("--batch-jobs", type=int, default=256)
+    ap.add_argument("--batch-max-seqs", type=int, default=200000)
     ap.add_argument("--n-seqs", type=int, default=0, help="override the sequence count (testing only)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--mode", default="graph", choices=["graph", "plain"])
@@ -381,14 +383,112 @@ def run_cpu_replicas(args, dist: Dist):
                           "config": workload_desc(args, cfg)}), flush=True)
 
 
+# ---- batch workload: many independent jobs -----------------------------------------
+def batch_jobs(args):
+    """256 seeded jobs: log-uniform 1,000-200,000 sequences each, DNA (lengths
+    log-uniform 100-10,000) or protein (the 200k-protein generator), similarity
+    drawn from {0.8, 0.9, 0.95}; returns [(db, params, description)]."""
+    import math
+
+    import numpy as np
+
+    import ngia
+
+    rng = np.random.default_rng(args.seed)
+    jobs = []
+    for j in range(args.batch_jobs):
+        t = int(rng.integers(0, 2))
+        n = int(round(math.exp(rng.uniform(math.log(1e3), math.log(args.batch_max_seqs)))))
+        s = float(rng.choice([0.8, 0.9, 0.95]))
+        if t == 0:
+            cfg = dict(type=0, len_dist=2, n_seqs=n, n_ancestors=max(1, n // 50), len_a=100.0, len_b=10000.0,
+                       len_min=100, len_max=10000, subst_max=0.20, indel_frac=0.05, indel_max=3)
+        else:
+            cfg = dict(type=1, len_dist=1, n_seqs=n, n_ancestors=max(1, n // 25), len_a=380.0, len_b=0.7,
+                       len_min=20, len_max=35000, subst_max=0.50, indel_frac=0.05, indel_max=5)
+        seqs = ngia.synth(**cfg, seed=args.seed * 100003 + j)
+        db = ngia.DB.pack(t, seqs, seqs.off)
+        seqs.close()
+        jobs.append((db, ngia.params_clamp(t, s, args.word, 0)))
+    return jobs
+
+
+def run_batch(args, dist: Dist):
+    """Batch arm: every step runs the first S greedy iterations of all jobs,
+    once as one batch (each job's CUDA graph launched on its own stream, one
+    wait for all) and once one job after the other with the plain host-loop
+    driver.  Both return every job's assignment to the host; timed on the
+    host clock around the call (it synchronises)."""
+    import numpy as np
+
+    import ngia
+
+    ngia.set_device(dist.local)
+    S = args.iters_per_step
+    t0 = time.perf_counter()
+    jobs = batch_jobs(args)
+    t_gen = time.perf_counter() - t0
+    dbs, params = [j[0] for j in jobs], [j[1] for j in jobs]
+    n_total = sum(db.n for db in dbs)
+    arms = {}
+    with ngia.Batch(dbs) as b:
+        for mode, name in ((ngia.MODE_GRAPH, "batch"), (ngia.MODE_PLAIN, "plain")):
+            for _ in range(args.warmup):
+                b.run(params, mode, max_iters=S)
+            dist.barrier()
+            clocks = Clocks(dist.local)
+            clocks.start()
+            cands = cells = 0
+            t = time.perf_counter()
+            for _ in range(args.steps):
+                cls, ids, st = b.run(params, mode, max_iters=S)
+                cands += st["candidates"]
+                cells += st["band_cells"]
+            T = dist.reduce(time.perf_counter() - t, "max")
+            arms[name] = dict(T=T, cands=dist.reduce(float(cands), "sum"), cells=dist.reduce(float(cells), "sum"),
+                              clk=clocks.stop(), out=(cls, ids))
+    same = all(np.array_equal(a, c) for a, c in zip(arms["batch"]["out"][0], arms["plain"]["out"][0])) and \
+        all(np.array_equal(a, c) for a, c in zip(arms["batch"]["out"][1], arms["plain"]["out"][1]))
+    for db in dbs:
+        db.close()
+    if dist.rank != 0:
+        return
+    bat, pln = arms["batch"], arms["plain"]
+    n_dna = sum(1 for db in dbs if db.type == 0)
+    out = {"metric": METRIC, "value": bat["cands"] / bat["T"], "unit": UNIT, "n_gpus": dist.world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * bat["T"] / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+           "data": "synthetic (seeded generators with the configuration's shapes)",
+           "config": {"workload": f"batch{args.batch_jobs}: {args.batch_jobs} independent jobs "
+                                  f"({n_dna} DNA, {args.batch_jobs - n_dna} protein), {n_total:,} sequences, "
+                                  f"log-uniform 1,000-{args.batch_max_seqs:,} per job, DNA lengths log-uniform "
+                                  f"100-10,000, protein log-normal(median 380, sigma 0.7), s in {{0.8,0.9,0.95}}, "
+                                  f"w={args.word} (clamped per job)",
+                      "iters_per_step": S, "step": f"first {S} greedy iterations of every job",
+                      "timing": "host clock around ngia_batch_run (assignments of all jobs returned to host)",
+                      "generation_s": round(t_gen, 1)},
+           "gcups": bat["cells"] / bat["T"] / 1e9,
+           "plain": {"value": pln["cands"] / pln["T"], "ms_per_step": 1e3 * pln["T"] / args.steps,
+                     "gcups": pln["cells"] / pln["T"] / 1e9,
+                     "form": "jobs one after the other, host loop per representative"},
+           "speedup_vs_plain": pln["T"] / bat["T"], "bit_exact_vs_plain": bool(same),
+           "clocks": bat["clk"], "plain_clocks": pln["clk"]}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload.startswith("batch"):
+        # one hardware queue per job stream (the default is 8)
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     dist = Dist()
     try:
         if args.cpu_only:
             run_cpu_replicas(args, dist)
         elif args.impl == "reference":
             run_reference(args, dist)
+        elif args.workload.startswith("batch"):
+            run_batch(args, dist)
         else:
             run_ours(args, dist)
     finally:
