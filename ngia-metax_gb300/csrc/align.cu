@@ -23,9 +23,10 @@
 //   registers shift down one slot; an entering block starts all-ones.  Lanes
 //   claim pairs from the class queue independently (warp-aggregated atomics).
 //
-// k_align_generic<P>  any band width: one thread per pair in the reference's
-//   (i, j, k) order with line[] in global scratch and the 32 column carries
-//   packed into one word.
+// k_align_tiled<P,RING>  wider windows: one thread per pair, the band rows
+//   in a ring (shared memory for windows up to RING = 64 or 128 blocks,
+//   global scratch for any width with RING = 0), updated tile by tile with
+//   the same generated instruction sequence.
 //
 // Both stop a pair early once it provably cannot reach the cutoff: each query
 // residue raises the counted zeros by at most one (the bit-vector update only
@@ -344,17 +345,41 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_
 // tile) and leave in `ncw` (ignored after the highest tile).  Slots past `je`
 // are padding: computed, never stored.  Returns the change of the tile's
 // zero count (all bits).
-template <int P, int TW, int RING>
-__device__ __forceinline__ int tiled_tile(uint32_t *ring, const uint32_t *s_pl, int base, int je, int cols,
+// Band rows of one lane's pair, indexed by absolute rep block j.  Windows of
+// up to RING blocks keep them in shared memory (row j of thread t at
+// (j mod RING) * threads + t: the 32 lanes of a warp hit 32 banks); wider
+// windows keep them in global scratch with the same layout over all lanes
+// of the grid (a warp's accesses to one row are one 128-byte line).
+template <int RING>
+struct SmemRing {
+  uint32_t *base;  // ring + threadIdx.x
+  __device__ __forceinline__ uint32_t &operator[](int j) const { return base[(j & (RING - 1)) * kAlignThreads]; }
+};
+struct GlobalRing {
+  uint32_t *base;  // scratch + global lane index
+  uint32_t mask;   // ring size - 1 (a power of two >= the widest window)
+  int64_t stride;  // lanes of the grid
+  __device__ __forceinline__ uint32_t &operator[](int j) const { return base[(int64_t)(j & mask) * stride]; }
+};
+template <int RING>
+struct RingOf {
+  using T = SmemRing<RING>;
+};
+template <>
+struct RingOf<0> {
+  using T = GlobalRing;
+};
+
+template <int P, int TW, class Ring>
+__device__ __forceinline__ int tiled_tile(const Ring &ring, const uint32_t *s_pl, int base, int je, int cols,
                                           const uint32_t (&cur)[P], uint32_t &cw, uint32_t &ncw) {
-  constexpr int RS = kAlignThreads;
   uint32_t row[TW], pl[P][TW];
   int zold = 0;
 #pragma unroll
   for (int m = 0; m < TW; m++) {
     const int j = base + m;
     const bool in = j <= je;
-    row[m] = in ? ring[(j & (RING - 1)) * RS] : 0u;
+    row[m] = in ? ring[j] : 0u;
     zold += in ? __popc(~row[m]) : 0;
 #pragma unroll
     for (int p = 0; p < P; p++) pl[p][m] = in ? s_pl[j * P + p] : 0u;
@@ -377,7 +402,7 @@ __device__ __forceinline__ int tiled_tile(uint32_t *ring, const uint32_t *s_pl, 
   for (int m = 0; m < TW; m++) {
     const int j = base + m;
     if (j <= je) {
-      ring[(j & (RING - 1)) * RS] = row[m];
+      ring[j] = row[m];
       znew += __popc(~row[m]);
     }
   }
@@ -385,13 +410,13 @@ __device__ __forceinline__ int tiled_tile(uint32_t *ring, const uint32_t *s_pl, 
 }
 
 // The last tile of a block row, exactly `rem` (1..MT-1, warp-uniform) slots wide.
-template <int P, int RING, int MT>
-__device__ __forceinline__ int tiled_rem(int rem, uint32_t *ring, const uint32_t *s_pl, int base, int je, int cols,
+template <int P, class Ring, int MT>
+__device__ __forceinline__ int tiled_rem(int rem, const Ring &ring, const uint32_t *s_pl, int base, int je, int cols,
                                          const uint32_t (&cur)[P], uint32_t &cw, uint32_t &ncw) {
   switch (rem) {
 #define NGIA_REM(W) \
   case W:           \
-    if (W < MT) return tiled_tile<P, (W < MT ? W : 1), RING>(ring, s_pl, base, je, cols, cur, cw, ncw); \
+    if (W < MT) return tiled_tile<P, (W < MT ? W : 1), Ring>(ring, s_pl, base, je, cols, cur, cw, ncw); \
     return 0;
     NGIA_REM(1) NGIA_REM(2) NGIA_REM(3) NGIA_REM(4) NGIA_REM(5) NGIA_REM(6) NGIA_REM(7) NGIA_REM(8)
     NGIA_REM(9) NGIA_REM(10) NGIA_REM(11) NGIA_REM(12) NGIA_REM(13) NGIA_REM(14) NGIA_REM(15) NGIA_REM(16)
@@ -403,10 +428,9 @@ __device__ __forceinline__ int tiled_rem(int rem, uint32_t *ring, const uint32_t
   }
 }
 
-// Tiled window: windows of up to RING rep blocks.  Each lane keeps its
-// pair's band rows in a shared-memory ring indexed by absolute rep block
-// (ring[(j mod RING) * threads + tid], so the 32 lanes of a warp hit 32
-// distinct banks whatever their j), and runs each query block tile by tile in
+// Tiled window: windows of up to RING rep blocks (any width for RING = 0).
+// Each lane keeps its pair's band rows in a ring indexed by absolute rep
+// block (SmemRing / GlobalRing above) and runs each query block tile by tile in
 // ascending rep-block order, all residues of the block per tile — the
 // reference's (i, j, k) loop order at tile granularity.  Full tiles are MT
 // slots (tiled_main); the remainder runs as one tile of exactly its width;
@@ -427,9 +451,20 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
   if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
-  uint32_t *ring = smem + (((db.max_nb * P + 3) & ~3) + kListWords) + threadIdx.x;
-  constexpr int RS = kAlignThreads;  // ring stride
   RunState *st = rb.st;
+  typename RingOf<RING>::T ring;
+  if constexpr (RING > 0) {
+    ring.base = smem + (((db.max_nb * P + 3) & ~3) + kListWords) + threadIdx.x;
+  } else {
+    const int64_t TL = (int64_t)gridDim.x * blockDim.x;
+    if ((int64_t)(rb.ring_mask + 1) * TL > rb.scratch_words) {
+      if (threadIdx.x == 0) set_error(st, NGIA_ERR_SCRATCH, 20);
+      return;
+    }
+    ring.base = rb.scratch + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    ring.mask = rb.ring_mask;
+    ring.stride = TL;
+  }
   const int lane = threadIdx.x & 31;
   const float s = prm.s;
   const int nb1 = h.nb1;
@@ -477,7 +512,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
         state = -1;
         busy = false;
       } else {
-        for (int j = 0; j <= je; j++) ring[(j & (RING - 1)) * RS] = 0xFFFFFFFFu;
+        for (int j = 0; j <= je; j++) ring[j] = 0xFFFFFFFFu;
 #pragma unroll
         for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
         active = true;
@@ -502,36 +537,36 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       uint32_t cw = 0, ncw = 0;
       int base = js;
       for (int t = 0; t < full; t++, base += MT) {
-        zw += tiled_tile<P, MT, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+        zw += tiled_tile<P, MT, typename RingOf<RING>::T>(ring, s_pl, base, je, cols, cur, cw, ncw);
         cw = ncw << (32 - cols);  // column 0's carry at bit 31
         ncw = 0;
       }
       for (; rem >= MT; rem -= MT, base += MT) {
-        zw += tiled_tile<P, MT, RING>(ring, s_pl, base, je, cols, cur, cw, ncw);
+        zw += tiled_tile<P, MT, typename RingOf<RING>::T>(ring, s_pl, base, je, cols, cur, cw, ncw);
         cw = ncw << (32 - cols);
         ncw = 0;
       }
-      if (rem > 0) zw += tiled_rem<P, RING, MT>(rem, ring, s_pl, base, je, cols, cur, cw, ncw);
+      if (rem > 0) zw += tiled_rem<P, typename RingOf<RING>::T, MT>(rem, ring, s_pl, base, je, cols, cur, cw, ncw);
     }
     i++;
     bool finished = i >= nq;
     if (!finished) {
       if (i - B > 0) {  // block js leaves the band
-        const uint32_t r0 = ring[(js & (RING - 1)) * RS];
+        const uint32_t r0 = ring[js];
         frozen += __popc(~r0 & (js == nb1 - 1 ? vlast : 0xFFFFFFFFu));
         zw -= __popc(~r0);
         js++;
       }
       if (i + B <= nb1 - 1) {  // block je enters all-ones
         je++;
-        ring[(je & (RING - 1)) * RS] = 0xFFFFFFFFu;
+        ring[je] = 0xFFFFFFFFu;
       }
       if (js > je) finished = true;
     }
     if (finished) {
       int sum = frozen;
       for (int j = js; j <= je; j++)
-        sum += __popc(~ring[(j & (RING - 1)) * RS] & (j == nb1 - 1 ? vlast : 0xFFFFFFFFu));
+        sum += __popc(~ring[j] & (j == nb1 - 1 ? vlast : 0xFFFFFFFFu));
       finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, sum, cutoff, L2, net2, qpl, s_list, n_members);
       active = false;
       state = -1;
@@ -548,96 +583,6 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
   flush_align_stats(st, n_pairs, n_members, n_cells, n_done);
 }
 
-template <int P>
-__global__ void __launch_bounds__(kAlignThreads) k_align_generic(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode) {
-  extern __shared__ __align__(16) uint32_t smem[];
-  __shared__ uint64_t bar;
-  AlignHdr h;
-  if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
-  const uint32_t *s_pl = smem;
-  const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
-  RunState *st = rb.st;
-  const int lane = threadIdx.x & 31;
-  const float s = prm.s;
-  const int nb1 = h.nb1;
-  const uint32_t vlast = (h.net1 & 31) ? ((1u << (h.net1 & 31)) - 1u) : 0xFFFFFFFFu;
-  const int64_t gl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int64_t TL = (int64_t)gridDim.x * blockDim.x;
-  if ((int64_t)nb1 * TL > rb.scratch_words) {
-    if (threadIdx.x == 0) set_error(st, NGIA_ERR_SCRATCH, 20);
-    return;
-  }
-  uint32_t *line = rb.scratch + gl;  // line[j] at line[j * TL]
-
-  int state = -1, entry = 0, cand = 0, i = 0, nq = 0, B = 0, net2 = 0, L2 = 0, cutoff = 0, zc = 0;
-  bool busy = false;
-  const uint32_t *qpl = nullptr;
-  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0, n_done = 0;
-  for (;;) {
-    claim(st, cls, h.qn, lane, state);
-    if (__all_sync(kFullMask, state == -2)) break;
-    if (state < 0) continue;
-    if (!busy) {
-      const int e = rb.queue[cls][state];
-      cand = score_mode ? rb.score_cands[e] : e;
-      entry = e;
-      L2 = db.len[cand];
-      net2 = db.net[cand];
-      nq = (net2 + 31) >> 5;
-      B = band_blocks(h.L1, L2, s);
-      cutoff = cutoff_of(L2, s);
-      qpl = db.words + db.off[cand] + db.hw;
-      if (!score_mode) {
-        n_pairs++;
-        n_cells += (unsigned long long)band_cells(B, nb1, net2);
-      }
-      for (int j = 0; j < nb1; j++) line[j * TL] = 0xFFFFFFFFu;
-      i = 0;
-      zc = 0;
-      busy = true;
-    }
-    if (i < nq) {
-      const int cols = ((i + 1) * 32 > net2) ? (net2 & 31) : 32;
-      uint32_t col[P];
-#pragma unroll
-      for (int p = 0; p < P; p++) col[p] = qpl[i * P + p];
-      const int jstart = max(i - B, 0), jend = min(i + B, nb1 - 1);
-      if (jend >= jstart) n_done += (unsigned long long)(jend - jstart + 1) * cols;
-      uint32_t cw = 0;
-      for (int j = jstart; j <= jend; j++) {
-        uint32_t R[P];
-#pragma unroll
-        for (int p = 0; p < P; p++) R[p] = s_pl[j * P + p];
-        const uint32_t old = line[j * TL];
-        uint32_t row = old, ncw = 0;
-        for (int k = 0; k < cols; k++) {
-          uint32_t x = row;
-#pragma unroll
-          for (int p = 0; p < P; p++) x &= ~(R[p] ^ (0u - ((col[p] >> k) & 1u)));
-          const unsigned long long tt = (unsigned long long)row + x + ((cw >> k) & 1u);
-          ncw |= (uint32_t)(tt >> 32) << k;
-          row = (uint32_t)tt | (row ^ x);
-        }
-        const uint32_t v = (j == nb1 - 1) ? vlast : 0xFFFFFFFFu;
-        zc += __popc(~row & v) - __popc(~old & v);
-        line[j * TL] = row;
-        cw = ncw;
-      }
-      i++;
-      if (!score_mode && i < nq && zc + (net2 - 32 * i) < cutoff) {
-        busy = false;
-        state = -1;
-        continue;
-      }
-    }
-    if (i >= nq) {
-      finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, zc, cutoff, L2, net2, qpl, s_list, n_members);
-      busy = false;
-      state = -1;
-    }
-  }
-  flush_align_stats(st, n_pairs, n_members, n_cells, n_done);
-}
 
 // ---- dispatch ---------------------------------------------------------------------
 typedef void (*AlignFn)(DevDB, RunBufs, RunParams, int, int);
@@ -651,7 +596,7 @@ static AlignFn align_fn(int type, int cls) {
       case 3: return k_align_win<2, 32>;
       case 4: return k_align_tiled<2, 64>;
       case 5: return k_align_tiled<2, 128>;
-      default: return k_align_generic<2>;
+      default: return k_align_tiled<2, 0>;
     }
   }
   switch (cls) {
@@ -659,7 +604,7 @@ static AlignFn align_fn(int type, int cls) {
     case 1: return k_align_win<5, 16>;
     case 2: return k_align_tiled<5, 64>;
     case 3: return k_align_tiled<5, 128>;
-    default: return k_align_generic<5>;
+    default: return k_align_tiled<5, 0>;
   }
 }
 

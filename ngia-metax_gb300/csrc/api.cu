@@ -268,7 +268,10 @@ int ngia::drv::open_ctx(const ngia_db_view *v, bool batch_member, ngia_ctx **out
   }
   const int g = ngia::generic_class(type);
   rb.generic_lanes = c->grid_align[g] * ngia::align_threads();
-  rb.scratch_words = (int64_t)rb.generic_lanes * c->db.max_nb;
+  uint32_t ring = 1;
+  while ((int)ring < c->db.max_nb) ring <<= 1;
+  rb.ring_mask = ring - 1;
+  rb.scratch_words = (int64_t)rb.generic_lanes * ring;
   if (dalloc(&rb.scratch, (size_t)rb.scratch_words) != cudaSuccess)
     return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation of alignment scratch failed"));
   if (cudaMallocHost((void **)&c->h_state, sizeof(ngia::RunState)) != cudaSuccess)

@@ -19,11 +19,12 @@ constexpr int kRefGridThreads = 128 * 128;     // BLOCK*WARP of the reference la
 // register-window classes hold the whole window in registers (capacity WC);
 // the tiled classes keep up to 64 or 128 window rows per pair in a
 // shared-memory ring and stream them through 16-slot register tiles; the last
-// class of each type is the generic kernel (any width).
+// class of each type (any width) runs the tiled kernel on a global-memory
+// ring.
 constexpr int kNumClasses = 7;
 constexpr int kRingBlocks = 128;  // largest ring (the tiled classes use 64 and 128)
 __host__ __device__ inline int class_cap(int type, int c) {
-  // DNA: 8,16,24,32 | tiled 64, 128 | generic;  protein: 8,16 | tiled 64, 128 | generic
+  // DNA: 8,16,24,32 | tiled 64, 128 | any;  protein: 8,16 | tiled 64, 128 | any
   if (type == 0) {
     const int caps[7] = {8, 16, 24, 32, 64, 128, 0};
     return caps[c];
@@ -109,9 +110,10 @@ struct RunBufs {
   int32_t *pos;           // position of a base survivor in the job list
   int32_t *first_short;   // per reference thread: first job with net < 16
   uint32_t *scan_part;    // scan partials
-  uint32_t *scratch;      // per-lane line storage of the generic kernel
+  uint32_t *scratch;      // per-lane band rows of the widest class (global ring)
   int64_t scratch_words;
   int32_t generic_lanes;
+  uint32_t ring_mask;     // global ring size - 1 (power of two >= the widest record)
   // filter counters, 32 stripes x kFilterStats (one 64-byte line each),
   // added per CTA and folded into the run state by k_next
   unsigned long long *fstats;
