@@ -199,8 +199,10 @@ typedef struct ngia_batch ngia_batch;
 int ngia_batch_open(const ngia_db_view *jobs, int32_t n_jobs, ngia_batch **out);
 
 /* Clusters every job with its own parameters (params[j], clamped).
- * NGIA_MODE_GRAPH: all jobs in one CUDA graph launch — one conditional while
- * node per job, no host round trip until the whole batch is done;
+ * NGIA_MODE_GRAPH: every job's whole greedy loop is one launch of its CUDA
+ * graph (a conditional while node); all launches are queued, each on the
+ * job's own stream, before the batch waits once, so jobs run side by side
+ * with no host round trip per representative;
  * NGIA_MODE_PLAIN: the jobs one after the other with the host-loop driver.
  * max_iters > 0 stops each job after that many representatives (sampling).
  * cluster_out[j] / identity_out[j] (either may be NULL) receive job j's
@@ -211,6 +213,75 @@ int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t mode,
                    int32_t **identity_out, ngia_stats *stats);
 
 int ngia_batch_close(ngia_batch *b);
+
+/* ---- serving: continuous batching against a resident representative set --
+ * No counterpart in the reference (its program clusters one database per
+ * run); the per-pair tests and thresholds are those of ngia_cluster.
+ * ngia_serve_open keeps a representative set resident on the GPU (records
+ * plus one k-mer bitset per representative).  Each submitted batch (a
+ * database of queries of the same type, in makeDB layout) is assigned
+ * against it: query q joins the first representative r, in the order of
+ * `reps` (their creation order), whose pair (r as representative, q as
+ * candidate) passes the composition test, the short-word test (when precise
+ * is 0 and both net lengths are >= 16) and the banded-LCS test:
+ * rep_out[q] = r, ident_out[q] = the banded-LCS score.  The queries no
+ * resident representative takes are then clustered among themselves exactly
+ * as ngia_cluster clusters a database holding only them: rep_out[q] = -1 - j,
+ * j = the batch index of q's new representative (ident_out[j] = -1).  The
+ * resident set never changes, so a batch's result does not depend on the
+ * batches around it.
+ *
+ * Batches run on `slots` workers side by side on the GPU, each with its own
+ * stream and device memory for batches of up to max_batch records,
+ * max_batch_words record words and records of max_record_blocks plane
+ * blocks (32 residues each).  A submitted batch waits in a FIFO until a
+ * slot is free; the slot count is capped so that all slots fit
+ * memory_budget bytes of device memory. */
+typedef struct ngia_server ngia_server;
+
+typedef struct ngia_serve_config {
+    int32_t slots;              /* workers (0 = 4)                              */
+    int32_t max_batch;          /* records per batch (0 = 4,096)                */
+    int32_t max_record_blocks;  /* plane blocks per query record (0 = 128)      */
+    int32_t reserved;
+    int64_t max_batch_words;    /* record words per batch (0 = max_batch x the  */
+                                /* words of a record of max_record_blocks)      */
+    int64_t memory_budget;      /* device bytes for all slots (0 = half free)   */
+} ngia_serve_config;
+
+typedef struct ngia_serve_result {
+    int32_t done;        /* 1 when the batch is finished (results written)      */
+    int32_t slot;        /* worker that ran it                                  */
+    int32_t rounds;      /* assignment rounds (chunks of representatives)       */
+    int32_t resident;    /* queries that joined a resident representative       */
+    int32_t new_reps;    /* representatives created among the leftovers         */
+    int32_t reserved;
+    double  queued_ms;   /* submit -> start on a slot                           */
+    double  run_ms;      /* start on a slot -> finished                         */
+} ngia_serve_result;
+
+/* Opens the service on the current device; params are clamped
+ * (ngia_params_clamp) and apply to every batch. */
+int ngia_serve_open(const ngia_db_view *reps, const ngia_params *params,
+                    const ngia_serve_config *cfg, ngia_server **out);
+
+/* Number of slots (batches that can run at the same time). */
+int ngia_serve_slots(const ngia_server *s, int32_t *slots);
+
+/* Queues a batch (copied; the caller may free it on return) and returns its
+ * ticket.  NGIA_E_LIMIT when the batch exceeds a slot's capacity. */
+int ngia_serve_submit(ngia_server *s, const ngia_db_view *batch, int64_t *ticket);
+
+/* Looks at a ticket, waiting up to wait_ms milliseconds for it (0 = do not
+ * wait, < 0 = until done).  When the batch is done: rep_out / ident_out
+ * (batch.n entries each, either may be NULL) receive the results, res->done
+ * is 1 and the ticket is released; otherwise res->done is 0.  A batch that
+ * failed returns its error code (and releases the ticket). */
+int ngia_serve_poll(ngia_server *s, int64_t ticket, int32_t wait_ms, int32_t *rep_out,
+                    int32_t *ident_out, ngia_serve_result *res);
+
+/* Finishes the queued and running batches, then frees the service. */
+int ngia_serve_close(ngia_server *s);
 
 /* Per-pair stage values for (rep, cands[k]) pairs, for unit-level parity:
  * out[4k+0] = composition sum, out[4k+1] = short-word count (-1 when the

@@ -170,6 +170,139 @@ int validate_params(int type, const ngia_params *p) {
 
 extern "C" int ngia_open(const ngia_db_view *v, ngia_ctx **out) { return ngia::drv::open_ctx(v, false, out); }
 
+namespace {
+
+using ngia::drv::dalloc;
+
+// Streams and events of a context.
+int create_streams(ngia_ctx *c) {
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) return fail(NGIA_E_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
+    return fail(NGIA_E_CUDA, "cannot query SM count");
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(NGIA_E_CUDA, "cannot create stream");
+  for (int k = 0; k < ngia::kNumClasses; k++) {
+    if (cudaStreamCreateWithFlags(&c->side[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
+      return fail(NGIA_E_CUDA, "cannot create side streams");
+  }
+  if (cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&c->ev_step0) != cudaSuccess || cudaEventCreate(&c->ev_step1) != cudaSuccess ||
+      cudaEventCreate(&c->ev_p0) != cudaSuccess || cudaEventCreate(&c->ev_p1) != cudaSuccess ||
+      cudaEventCreate(&c->ev_p2) != cudaSuccess)
+    return fail(NGIA_E_CUDA, "cannot create event");
+  for (auto &ev : c->ev_cls)
+    if (cudaEventCreate(&ev) != cudaSuccess) return fail(NGIA_E_CUDA, "cannot create event");
+  if (dalloc(&c->d_flags, 3) != cudaSuccess || cudaMallocHost((void **)&c->h_flags, 3 * sizeof(int32_t)) != cudaSuccess)
+    return fail(NGIA_E_NOMEM, "ngia_open: allocation failed");
+  if (cudaMallocHost((void **)&c->h_state, sizeof(ngia::RunState)) != cudaSuccess)
+    return fail(NGIA_E_NOMEM, "ngia_open: pinned allocation failed");
+  std::memset(c->h_state, 0, sizeof(ngia::RunState));
+  return NGIA_OK;
+}
+
+// Device arrays of a database of up to cap_n records and cap_words words.
+int alloc_db(ngia_ctx *c, int type, int64_t cap_n, int64_t cap_words) {
+  const int A = ngia::count_words(type);
+  if (dalloc(&c->d_words, (size_t)cap_words + 4) != cudaSuccess || dalloc(&c->d_off, (size_t)cap_n) != cudaSuccess ||
+      dalloc(&c->d_len, (size_t)cap_n) != cudaSuccess || dalloc(&c->d_net, (size_t)cap_n) != cudaSuccess ||
+      dalloc(&c->d_cnt, (size_t)cap_n * A) != cudaSuccess)
+    return fail(NGIA_E_NOMEM, "ngia_open: device allocation of the database failed");
+  c->cap_n = cap_n;
+  c->cap_words = cap_words;
+  c->db.words = c->d_words;
+  c->db.off = c->d_off;
+  c->db.len = c->d_len;
+  c->db.net = c->d_net;
+  c->db.cnt = c->d_cnt;
+  c->db.n = 0;
+  c->db.type = type;
+  c->db.hw = ngia::header_words(type);
+  c->db.P = ngia::plane_count(type);
+  c->db.A = A;
+  c->db.max_nb = 1;
+  return NGIA_OK;
+}
+
+// Copies a database view into the context's arrays (one host-to-device copy
+// of the records and offsets) and builds the header arrays on the device.
+int load_db(ngia_ctx *c, const ngia_db_view *v) {
+  cudaError_t e =
+      cudaMemcpyAsync(c->d_words, v->words, sizeof(uint32_t) * (size_t)v->n_words, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(c->d_off, v->rec_off, sizeof(int64_t) * (size_t)v->n, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->d_flags, 0, 3 * sizeof(int32_t), c->stream);
+  if (e != cudaSuccess) return fail(NGIA_E_CUDA, "ngia_open: copy: %s", cudaGetErrorString(e));
+  c->n_words = v->n_words;
+  c->longest = v->longest;
+  c->db.n = v->n;
+  e = ngia::launch_loader(c, c->d_flags, c->d_flags + 1, c->d_flags + 2);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(c->h_flags, c->d_flags, 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return fail(NGIA_E_CUDA, "ngia_open: loader: %s", cudaGetErrorString(e));
+  if (c->h_flags[2]) return fail(NGIA_E_FORMAT, "ngia_open: a record offset or header is out of range");
+  c->db.max_nb = std::max(1, c->h_flags[0]);
+  c->db.has_short = c->h_flags[1];
+  return NGIA_OK;
+}
+
+// Launch grids for the loaded database: persistent grids over the whole GPU,
+// or (batch members and serving slots, which share the GPU with other jobs)
+// one CTA per 128 candidates and one warp per bitmap word.
+void size_grids(ngia_ctx *c, bool by_size) {
+  const int type = c->db.type;
+  for (int k = 0; k < ngia::num_classes(type); k++)
+    c->grid_align[k] = c->num_sms * ngia::align_occupancy(type, k, c->cap_nb);
+  c->grid_filter = c->num_sms * 8;
+  if (by_size) {
+    const int64_t n = std::max(1, c->db.n), nbw = (n + 31) / 32;
+    const int by_n = (int)std::min<int64_t>((n + 127) / 128, INT32_MAX);
+    for (int k = 0; k < ngia::num_classes(type); k++) c->grid_align[k] = std::max(1, std::min(c->grid_align[k], by_n));
+    c->grid_filter = std::max(1, std::min(c->grid_filter, (int)((nbw + 7) / 8)));
+  }
+}
+
+// Run buffers for up to cap_n sequences whose records have up to cap_nb
+// plane blocks (grids sized for that capacity).
+int alloc_run(ngia_ctx *c, int64_t cap_n, int cap_nb) {
+  const int type = c->db.type;
+  c->cap_nb = std::max(1, cap_nb);
+  const size_t nbw = (size_t)(cap_n + 31) / 32;
+  ngia::RunBufs &rb = c->rb;
+  bool ok = dalloc(&rb.st, 1) == cudaSuccess && dalloc(&rb.cluster, (size_t)cap_n) == cudaSuccess &&
+            dalloc(&rb.ident, (size_t)cap_n) == cudaSuccess && dalloc(&rb.alive, nbw) == cudaSuccess &&
+            dalloc(&rb.rep_rec, 32 + (size_t)ngia::kMaxBlocks * 5 + 64) == cudaSuccess &&
+            dalloc(&rb.rep_list, ngia::kListWords) == cudaSuccess &&
+            dalloc(&rb.first_short, ngia::kRefGridThreads) == cudaSuccess &&
+            dalloc(&rb.scan_part, nbw) == cudaSuccess;
+  ok = ok && cudaMalloc((void **)&rb.flags, 4 * std::max<size_t>(nbw, 1)) == cudaSuccess;
+  ok = ok && dalloc(&rb.fstats, (size_t)ngia::kFilterStripes * ngia::kFilterStats) == cudaSuccess;
+  for (int k = 0; ok && k < ngia::num_classes(type); k++) ok = dalloc(&rb.queue[k], (size_t)cap_n) == cudaSuccess;
+  if (!ok) return fail(NGIA_E_NOMEM, "ngia_open: device allocation of run buffers failed");
+  cudaMemsetAsync(rb.rep_list, 0, 4 * ngia::kListWords, c->stream);
+  cudaMemsetAsync(rb.fstats, 0, 8 * ngia::kFilterStripes * ngia::kFilterStats, c->stream);
+  if (ngia::align_configure(type, c->cap_nb) != cudaSuccess || ngia::filter_configure() != cudaSuccess)
+    return fail(NGIA_E_CUDA, "ngia_open: kernel attributes");
+  // the widest class keeps its rows in global scratch, sized for this
+  // context's grid at capacity (every later grid of the context is within)
+  const int32_t saved_n = c->db.n;
+  c->db.n = (int32_t)cap_n;
+  size_grids(c, c->batch_member);
+  c->db.n = saved_n;
+  const int g = ngia::generic_class(type);
+  rb.generic_lanes = c->grid_align[g] * ngia::align_threads();
+  uint32_t ring = 1;
+  while ((int)ring < c->cap_nb) ring <<= 1;
+  rb.ring_mask = ring - 1;
+  rb.scratch_words = (int64_t)rb.generic_lanes * ring;
+  if (dalloc(&rb.scratch, (size_t)rb.scratch_words) != cudaSuccess)
+    return fail(NGIA_E_NOMEM, "ngia_open: device allocation of alignment scratch failed");
+  return NGIA_OK;
+}
+
+}  // namespace
+
 int ngia::drv::open_ctx(const ngia_db_view *v, bool batch_member, ngia_ctx **out) {
   ngia::clear_error();
   if (!v || !out) return fail(NGIA_E_ARG, "ngia_open: null argument");
@@ -179,108 +312,58 @@ int ngia::drv::open_ctx(const ngia_db_view *v, bool batch_member, ngia_ctx **out
   if (!c) return fail(NGIA_E_NOMEM, "ngia_open: out of host memory");
   c->batch_member = batch_member;
   *out = nullptr;
-  int rc = NGIA_OK;
-  auto bail = [&](int r) {
+  int rc = create_streams(c);
+  if (!rc) rc = alloc_db(c, v->type, v->n, v->n_words);
+  if (!rc) rc = load_db(c, v);
+  if (!rc) rc = alloc_run(c, v->n, c->db.max_nb);
+  if (!rc) {
+    size_grids(c, batch_member);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = fail(NGIA_E_CUDA, "ngia_open: %s", cudaGetErrorString(e));
+  }
+  if (rc) {
     ngia_close(c);
-    return r;
-  };
-  cudaError_t e = cudaGetDevice(&c->device);
-  if (e != cudaSuccess) return bail(fail(NGIA_E_CUDA, "no CUDA device: %s", cudaGetErrorString(e)));
-  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess)
-    return bail(fail(NGIA_E_CUDA, "cannot query SM count"));
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
-    return bail(fail(NGIA_E_CUDA, "cannot create stream"));
-  for (int k = 0; k < ngia::kNumClasses; k++) {
-    if (cudaStreamCreateWithFlags(&c->side[k], cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&c->join_ev[k], cudaEventDisableTiming) != cudaSuccess)
-      return bail(fail(NGIA_E_CUDA, "cannot create side streams"));
+    return rc;
   }
-  if (cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreate(&c->ev_step0) != cudaSuccess || cudaEventCreate(&c->ev_step1) != cudaSuccess ||
-      cudaEventCreate(&c->ev_p0) != cudaSuccess || cudaEventCreate(&c->ev_p1) != cudaSuccess ||
-      cudaEventCreate(&c->ev_p2) != cudaSuccess)
-    return bail(fail(NGIA_E_CUDA, "cannot create event"));
-  for (auto &ev : c->ev_cls)
-    if (cudaEventCreate(&ev) != cudaSuccess) return bail(fail(NGIA_E_CUDA, "cannot create event"));
-  const int64_t n = v->n;
-  const int type = v->type;
-  const int A = ngia::count_words(type);
-  c->n_words = v->n_words;
-  c->longest = v->longest;
-  // database: one host-to-device copy of the packed records and offsets
-  if (dalloc(&c->d_words, (size_t)v->n_words + 4) != cudaSuccess || dalloc(&c->d_off, (size_t)n) != cudaSuccess ||
-      dalloc(&c->d_len, (size_t)n) != cudaSuccess || dalloc(&c->d_net, (size_t)n) != cudaSuccess ||
-      dalloc(&c->d_cnt, (size_t)n * A) != cudaSuccess)
-    return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation of the database failed"));
-  e = cudaMemcpyAsync(c->d_words, v->words, sizeof(uint32_t) * (size_t)v->n_words, cudaMemcpyHostToDevice, c->stream);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(c->d_off, v->rec_off, sizeof(int64_t) * (size_t)n, cudaMemcpyHostToDevice, c->stream);
-  if (e != cudaSuccess) return bail(fail(NGIA_E_CUDA, "ngia_open: copy: %s", cudaGetErrorString(e)));
-  int32_t *d_flags = nullptr;
-  if (dalloc(&d_flags, 3) != cudaSuccess) return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation failed"));
-  cudaMemsetAsync(d_flags, 0, 3 * sizeof(int32_t), c->stream);
-  c->db.words = c->d_words;
-  c->db.off = c->d_off;
-  c->db.len = c->d_len;
-  c->db.net = c->d_net;
-  c->db.cnt = c->d_cnt;
-  c->db.n = (int32_t)n;
-  c->db.type = type;
-  c->db.hw = ngia::header_words(type);
-  c->db.P = ngia::plane_count(type);
-  c->db.A = A;
-  e = ngia::launch_loader(c, d_flags, d_flags + 1, d_flags + 2);
-  int32_t h_flags[3] = {0, 0, 0};
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h_flags, d_flags, sizeof(h_flags), cudaMemcpyDeviceToHost, c->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-  cudaFree(d_flags);
-  if (e != cudaSuccess) return bail(fail(NGIA_E_CUDA, "ngia_open: loader: %s", cudaGetErrorString(e)));
-  if (h_flags[2]) return bail(fail(NGIA_E_FORMAT, "ngia_open: a record offset or header is out of range"));
-  c->db.max_nb = std::max(1, h_flags[0]);
-  c->db.has_short = h_flags[1];
-  // run buffers
-  const size_t nbw = (size_t)(n + 31) / 32;
-  ngia::RunBufs &rb = c->rb;
-  bool ok = dalloc(&rb.st, 1) == cudaSuccess && dalloc(&rb.cluster, (size_t)n) == cudaSuccess &&
-            dalloc(&rb.ident, (size_t)n) == cudaSuccess && dalloc(&rb.alive, nbw) == cudaSuccess &&
-            dalloc(&rb.rep_rec, 32 + (size_t)ngia::kMaxBlocks * 5 + 64) == cudaSuccess &&
-            dalloc(&rb.rep_list, ngia::kListWords) == cudaSuccess &&
-            dalloc(&rb.first_short, ngia::kRefGridThreads) == cudaSuccess &&
-            dalloc(&rb.scan_part, nbw) == cudaSuccess;
-  ok = ok && cudaMalloc((void **)&rb.flags, 4 * std::max<size_t>(nbw, 1)) == cudaSuccess;
-  ok = ok && dalloc(&rb.fstats, (size_t)ngia::kFilterStripes * ngia::kFilterStats) == cudaSuccess;
-  for (int k = 0; ok && k < ngia::num_classes(type); k++) ok = dalloc(&rb.queue[k], (size_t)n) == cudaSuccess;
-  if (!ok) return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation of run buffers failed"));
-  cudaMemsetAsync(rb.rep_list, 0, 4 * ngia::kListWords, c->stream);
-  cudaMemsetAsync(rb.fstats, 0, 8 * ngia::kFilterStripes * ngia::kFilterStats, c->stream);
-  // launch shapes
-  if (ngia::align_configure(type, c->db.max_nb) != cudaSuccess || ngia::filter_configure() != cudaSuccess)
-    return bail(fail(NGIA_E_CUDA, "ngia_open: kernel attributes"));
-  for (int k = 0; k < ngia::num_classes(type); k++)
-    c->grid_align[k] = c->num_sms * ngia::align_occupancy(type, k, c->db.max_nb);
-  c->grid_filter = c->num_sms * 8;
-  if (batch_member) {
-    // a batch runs many jobs side by side: size each job's grids to its own
-    // sequence count (one CTA per 128 candidates, one warp per bitmap word)
-    const int by_n = (int)std::min<int64_t>((n + 127) / 128, INT32_MAX);
-    for (int k = 0; k < ngia::num_classes(type); k++) c->grid_align[k] = std::max(1, std::min(c->grid_align[k], by_n));
-    c->grid_filter = std::max(1, std::min(c->grid_filter, (int)((nbw + 7) / 8)));
-  }
-  const int g = ngia::generic_class(type);
-  rb.generic_lanes = c->grid_align[g] * ngia::align_threads();
-  uint32_t ring = 1;
-  while ((int)ring < c->db.max_nb) ring <<= 1;
-  rb.ring_mask = ring - 1;
-  rb.scratch_words = (int64_t)rb.generic_lanes * ring;
-  if (dalloc(&rb.scratch, (size_t)rb.scratch_words) != cudaSuccess)
-    return bail(fail(NGIA_E_NOMEM, "ngia_open: device allocation of alignment scratch failed"));
-  if (cudaMallocHost((void **)&c->h_state, sizeof(ngia::RunState)) != cudaSuccess)
-    return bail(fail(NGIA_E_NOMEM, "ngia_open: pinned allocation failed"));
-  std::memset(c->h_state, 0, sizeof(ngia::RunState));
-  e = cudaStreamSynchronize(c->stream);
-  if (e != cudaSuccess) return bail(fail(NGIA_E_CUDA, "ngia_open: %s", cudaGetErrorString(e)));
-  (void)rc;
   *out = c;
+  return NGIA_OK;
+}
+
+int ngia::drv::open_ctx_capacity(int type, int64_t cap_n, int64_t cap_words, int cap_nb, ngia_ctx **out) {
+  if (!out || (type != 0 && type != 1) || cap_n <= 0 || cap_words <= 0 || cap_nb <= 0 || cap_nb > ngia::kMaxBlocks)
+    return fail(NGIA_E_ARG, "open_ctx_capacity: bad argument");
+  ngia_ctx *c = new (std::nothrow) ngia_ctx();
+  if (!c) return fail(NGIA_E_NOMEM, "out of host memory");
+  c->batch_member = true;
+  *out = nullptr;
+  int rc = create_streams(c);
+  if (!rc) rc = alloc_db(c, type, cap_n, cap_words);
+  if (!rc) rc = alloc_run(c, cap_n, cap_nb);
+  if (!rc) {
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) rc = fail(NGIA_E_CUDA, "open_ctx_capacity: %s", cudaGetErrorString(e));
+  }
+  if (rc) {
+    ngia_close(c);
+    return rc;
+  }
+  *out = c;
+  return NGIA_OK;
+}
+
+int ngia::drv::reload_ctx(ngia_ctx *c, const ngia_db_view *v) {
+  if (!c || !v || v->type != c->db.type || v->n <= 0 || !v->words || !v->rec_off || v->n_words <= 0)
+    return fail(NGIA_E_ARG, "reload: bad database view");
+  if (v->n > c->cap_n || v->n_words > c->cap_words)
+    return fail(NGIA_E_LIMIT, "reload: %d records / %lld words exceed the capacity (%lld / %lld)", v->n,
+                (long long)v->n_words, (long long)c->cap_n, (long long)c->cap_words);
+  destroy_graph(c);  // kernel arguments captured in a graph hold the old sizes
+  c->begun = false;
+  int rc = load_db(c, v);
+  if (rc) return rc;
+  if (c->db.max_nb > c->cap_nb)
+    return fail(NGIA_E_LIMIT, "reload: a record of %d blocks exceeds the capacity of %d", c->db.max_nb, c->cap_nb);
+  size_grids(c, true);
   return NGIA_OK;
 }
 
@@ -307,6 +390,8 @@ extern "C" int ngia_close(ngia_ctx *c) {
   cudaFree(rb.scratch);
   for (int k = 0; k < ngia::kNumClasses; k++) cudaFree(rb.queue[k]);
   if (c->h_state) cudaFreeHost(c->h_state);
+  cudaFree(c->d_flags);
+  if (c->h_flags) cudaFreeHost(c->h_flags);
   for (int k = 0; k < ngia::kNumClasses; k++) {
     if (c->side[k]) cudaStreamDestroy(c->side[k]);
     if (c->join_ev[k]) cudaEventDestroy(c->join_ev[k]);
@@ -332,8 +417,13 @@ extern "C" int ngia_device_count(int32_t *count) {
 }
 
 extern "C" int ngia_cluster_begin(ngia_ctx *c, const ngia_params *p, int32_t mode) {
+  return ngia::drv::begin_subset(c, p, mode, nullptr);
+}
+
+int ngia::drv::begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, const uint32_t *d_alive) {
   ngia::clear_error();
   if (!c) return fail(NGIA_E_ARG, "ngia_cluster_begin: null context");
+  if (c->db.n <= 0) return fail(NGIA_E_STATE, "ngia_cluster_begin: no database loaded");
   int rc = validate_params(c->db.type, p);
   if (rc) return rc;
   if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH) return fail(NGIA_E_ARG, "unknown mode %d", mode);
@@ -350,6 +440,7 @@ extern "C" int ngia_cluster_begin(ngia_ctx *c, const ngia_params *p, int32_t mod
   for (double &m : c->ms_class) m = 0.0;
   c->last_step_ms = 0.f;
   CK(ngia::launch_init_run(c));
+  if (d_alive) CK(ngia::launch_subset_start(c, d_alive));
   rc = pull_state(c);
   if (rc) return rc;
   if (mode == NGIA_MODE_GRAPH && !(c->graph_ready && same_params(c->graph_prm, c->prm))) {
@@ -379,6 +470,8 @@ extern "C" int ngia_cluster_step(ngia_ctx *c, int64_t max_iters, int32_t *done) 
   } else {
     CK(cudaEventRecord(c->ev_step0, c->stream));
     for (int64_t it = 0; max_iters <= 0 || it < max_iters; it++) {
+      if (it > (int64_t)c->db.n)  // every iteration retires one representative
+        return fail(NGIA_E_STATE, "ngia_cluster_step: more iterations than sequences");
       int rc = enqueue_iteration(c, false, 0);
       if (rc) return rc;
       rc = pull_state(c);  // the per-representative host round trip of the plain form

@@ -18,6 +18,12 @@ struct ngia_ctx {
   uint32_t *d_cnt = nullptr;
   int64_t n_words = 0;
   int32_t longest = 0;
+  // capacity of the allocations (a context can be reloaded with any database
+  // within it: serving slots)
+  int64_t cap_n = 0, cap_words = 0;
+  int32_t cap_nb = 0;
+  int32_t *d_flags = nullptr;  // loader results: max blocks, short record, bad record
+  int32_t *h_flags = nullptr;  // pinned mirror
   // run buffers
   ngia::RunBufs rb{};
   ngia::RunState *h_state = nullptr;  // pinned mirror
@@ -47,6 +53,15 @@ namespace ngia {
 // api.cu: driver internals shared with batch.cu / serve.cu
 namespace drv {
 int open_ctx(const ngia_db_view *v, bool batch_member, ngia_ctx **out);
+// A context with room for cap_n records, cap_words record words and records
+// of up to cap_nb plane blocks, holding no database until reload_ctx.
+int open_ctx_capacity(int type, int64_t cap_n, int64_t cap_words, int cap_nb, ngia_ctx **out);
+// Loads a database within the capacity (stream-ordered copies on the
+// context's stream; waits for that stream only).
+int reload_ctx(ngia_ctx *c, const ngia_db_view *v);
+// begin a run whose unclustered set is the given device bitmap (bit i =
+// sequence i takes part), instead of every sequence.
+int begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, const uint32_t *d_alive);
 int pull_state(ngia_ctx *c);
 int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond);
 void fill_stats(const ngia_ctx *c, ngia_stats *stats);
@@ -58,6 +73,7 @@ cudaError_t launch_init_run(ngia_ctx *c);
 cudaError_t launch_prep(ngia_ctx *c, int score_rep);
 cudaError_t launch_filter(ngia_ctx *c);
 cudaError_t launch_next(ngia_ctx *c, unsigned long long cond_handle, int use_cond);
+cudaError_t launch_subset_start(ngia_ctx *c, const uint32_t *d_alive);
 cudaError_t launch_score_classify(ngia_ctx *c, int n);
 // align.cu
 cudaError_t launch_align(ngia_ctx *c, int cls, cudaStream_t s, int score_mode);

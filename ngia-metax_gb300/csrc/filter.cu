@@ -14,6 +14,7 @@
 #include <climits>
 
 #include "ctx.h"
+#include "kmer.cuh"
 
 namespace ngia {
 
@@ -96,16 +97,6 @@ cudaError_t launch_init_run(ngia_ctx *c) {
 }
 
 // ---- representative preparation ----------------------------------------------
-// Residue code of net position q of a record's planes.
-template <int P>
-__device__ __forceinline__ uint32_t code_at(const uint32_t *planes, int q) {
-  const uint32_t *b = planes + (q >> 5) * P;
-  uint32_t c = 0;
-#pragma unroll
-  for (int p = 0; p < P; p++) c |= ((b[p] >> (q & 31)) & 1u) << p;
-  return c;
-}
-
 // Rep buffer layout: header words at [0, hw), planes from word kRepPlanes
 // (16-byte aligned for the bulk copy).
 constexpr int kRepPlanes = 32;
@@ -170,29 +161,6 @@ __global__ void k_prep(DevDB db, RunBufs rb, RunParams prm, int score_rep) {
 cudaError_t launch_prep(ngia_ctx *c, int score_rep) {
   k_prep<<<1, 512, 0, c->stream>>>(c->db, c->rb, c->prm, score_rep);
   return cudaGetLastError();
-}
-
-// ---- short-word count of one candidate (kernel_wordFilter job body) ----------
-template <int P>
-__device__ int word_count(const uint32_t *__restrict__ planes, int net2, int w, const uint32_t *list) {
-  constexpr int bits = P == 2 ? 2 : 5;
-  const uint32_t mask = (1u << (w * bits)) - 1u;
-  uint32_t word = 0;
-  int sum = 0;
-  for (int i = 0; i < net2; i += 32) {
-    uint32_t pl[P];
-#pragma unroll
-    for (int p = 0; p < P; p++) pl[p] = __ldg(planes + (i >> 5) * P + p);
-    const int lim = min(32, net2 - i);
-    for (int j = 0; j < lim; j++) {
-      uint32_t c = 0;
-#pragma unroll
-      for (int p = 0; p < P; p++) c |= ((pl[p] >> j) & 1u) << p;
-      word = ((word << bits) | c) & mask;
-      if (i + j >= w - 1) sum += (list[word >> 5] >> (word & 31)) & 1u;
-    }
-  }
-  return sum;
 }
 
 // ---- fast short-word count (filter stage) --------------------------------------
@@ -389,23 +357,6 @@ __device__ int word_count_warp(const uint32_t *__restrict__ planes, int net2, in
 // Candidates longer than this are counted by the whole warp.
 constexpr int kWarpWordLen = 2048;
 
-// Composition sum of candidate c against the representative counts rc[].
-template <int A>
-__device__ __forceinline__ int base_sum(const uint32_t *__restrict__ cnt, int c, const uint32_t *rc) {
-  int sum = 0;
-  if (A == 4) {
-    const uint4 q = __ldg(reinterpret_cast<const uint4 *>(cnt) + c);
-    sum = (int)(min(q.x, rc[0]) + min(q.y, rc[1]) + min(q.z, rc[2]) + min(q.w, rc[3]));
-  } else {
-    const uint4 *q4 = reinterpret_cast<const uint4 *>(cnt + (int64_t)c * 28);
-#pragma unroll
-    for (int k = 0; k < 7; k++) {
-      const uint4 q = __ldg(q4 + k);
-      sum += (int)(min(q.x, rc[4 * k]) + min(q.y, rc[4 * k + 1]) + min(q.z, rc[4 * k + 2]) + min(q.w, rc[4 * k + 3]));
-    }
-  }
-  return sum;
-}
 
 // Pushes candidate `c` of lane into work queue `cls` with one atomic per
 // class and warp (warp-aggregated compaction).
@@ -821,6 +772,45 @@ __global__ void k_next(DevDB db, RunBufs rb, unsigned long long cond, int use_co
       cudaGraphSetConditional((cudaGraphConditionalHandle)cond, more ? 1u : 0u);
     }
   }
+}
+
+// Start of a run over a subset of the sequences (the unclustered set was
+// loaded into rb.alive): the first member of the subset is the first
+// representative; an empty subset is done at once.
+__global__ void k_subset_start(DevDB db, RunBufs rb) {
+  RunState *st = rb.st;
+  __shared__ int s_min[32];
+  const int nbw = (db.n + 31) / 32;
+  int v = INT_MAX;
+  for (int wi = threadIdx.x; wi < nbw; wi += blockDim.x)
+    if (rb.alive[wi]) {
+      v = wi;
+      break;
+    }
+  for (int o = 16; o; o >>= 1) v = min(v, __shfl_xor_sync(kFullMask, v, o));
+  if ((threadIdx.x & 31) == 0) s_min[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    int u = threadIdx.x < (int)(blockDim.x >> 5) ? s_min[threadIdx.x] : INT_MAX;
+    for (int o = 16; o; o >>= 1) u = min(u, __shfl_xor_sync(kFullMask, u, o));
+    if (threadIdx.x == 0) {
+      if (u == INT_MAX) {
+        st->done = 1;
+      } else {
+        st->rep = u * 32 + __ffs(rb.alive[u]) - 1;
+        st->done = 0;
+      }
+    }
+  }
+}
+
+cudaError_t launch_subset_start(ngia_ctx *c, const uint32_t *d_alive) {
+  const int nbw = (c->db.n + 31) / 32;
+  cudaError_t e = cudaMemcpyAsync(c->rb.alive, d_alive, sizeof(uint32_t) * (size_t)nbw, cudaMemcpyDeviceToDevice,
+                                  c->stream);
+  if (e != cudaSuccess) return e;
+  k_subset_start<<<1, 1024, 0, c->stream>>>(c->db, c->rb);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_next(ngia_ctx *c, unsigned long long cond, int use_cond) {

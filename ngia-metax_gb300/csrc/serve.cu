@@ -1,0 +1,811 @@
+// serve.cu — continuous-batching service: query batches are assigned to a
+// resident representative set, then each batch's leftovers are clustered
+// among themselves.  The reference has no serving mode; the per-pair tests
+// are its own (composition, func.cu:323-354; short words, 357-447; banded
+// LCS, 450-604), applied with the representative in the reference role.
+//
+// Resident state (ngia_serve_open): the representatives as a device
+// database (records and header arrays, loaded by the same loader as
+// ngia_open) plus one k-mer bitset per representative, built on the device.
+//
+// One batch runs on one slot — a context of fixed capacity with its own
+// stream, driven by its own host thread:
+//  1. assignment, in rounds over chunks of representatives in creation order
+//     (64, 128, then 256 at a time): k_serve_filter tests every unassigned
+//     query against every representative of the chunk (composition, and the
+//     short-word test when it goes first) and queues the surviving pairs by
+//     band-window width; k_serve_align runs the banded LCS of each pair with
+//     the tiled register update (tile.cuh, lanes in lockstep) and keeps per
+//     query the smallest accepting representative with its score (one 64-bit
+//     atomicMin of rep << 32 | score); k_serve_round_end drops assigned
+//     queries and counts the rest.  A later round only holds later
+//     representatives, so a query assigned in a round is final and the
+//     rounds stop once no query is left (or the set is exhausted);
+//  2. the leftovers are clustered by the greedy driver over the batch's
+//     database restricted to them (begin_subset), which equals clustering a
+//     database of only the leftovers.
+// Slots run side by side on the GPU; a batch waits in a FIFO until a slot is
+// free.  The number of slots is capped by the memory budget.
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cstdio>
+#include <cstdlib>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../host/host_common.h"
+#include "ctx.h"
+#include "kmer.cuh"
+#include "tile.cuh"
+
+using ngia::fail;
+
+namespace ngia {
+namespace {
+
+constexpr int kServeClasses = 3;    // band windows <= 64 blocks, <= 128, wider
+constexpr int kFirstChunk = 64;     // representatives in the first round
+constexpr int kMaxChunk = 256;      // ... doubling up to this many per round
+constexpr unsigned long long kNoRep = ~0ull;
+
+// Device view of the resident representatives.
+struct RepStore {
+  const uint32_t *words;
+  const int64_t *off;
+  const int32_t *len, *net;
+  const uint32_t *cnt;
+  const uint32_t *lists;  // n x list_words k-mer bitsets (empty when net < 16)
+  int32_t n, list_words;
+};
+
+// Buffers of the assignment rounds of one slot.
+struct RoundBufs {
+  int2 *queue[kServeClasses];  // (representative, query) pairs of a round
+  uint32_t *ctl;               // [0..2] pairs queued per class, [3..5] claimed, [6] queries left
+  unsigned long long *key;     // per query: rep << 32 | score of the best accepting rep
+  uint32_t *todo;              // bitmap of the queries not assigned yet
+  int64_t cap;                 // pairs per class queue
+};
+
+__host__ __device__ inline int serve_class(int A) { return A <= 64 ? 0 : A <= 128 ? 1 : 2; }
+
+// k-mer presence bitset of every representative (the list of k_prep).
+template <int P>
+__global__ void k_rep_lists(RepStore rs, int w, uint32_t *lists) {
+  __shared__ uint32_t s_list[kListWords];
+  const int r = blockIdx.x;
+  const int lw = rs.list_words;
+  for (int i = threadIdx.x; i < lw; i += blockDim.x) s_list[i] = 0;
+  __syncthreads();
+  const uint32_t *rec = rs.words + rs.off[r];
+  const int net1 = (int)rec[1];
+  if (net1 >= 16) {
+    constexpr int bits = P == 2 ? 2 : 5;
+    const uint32_t mask = (1u << (w * bits)) - 1u;
+    const uint32_t *planes = rec + (P == 2 ? 6 : 30);
+    for (int p = w - 1 + threadIdx.x; p < net1; p += blockDim.x) {
+      uint32_t word = 0;
+      for (int t = p - w + 1; t <= p; t++) word = (word << bits) | code_at<P>(planes, t);
+      word &= mask;
+      atomicOr(&s_list[word >> 5], 1u << (word & 31));
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < lw; i += blockDim.x) lists[(int64_t)r * lw + i] = s_list[i];
+}
+
+__global__ void k_serve_init(int n, RoundBufs rb) {
+  const int nbw = (n + 31) / 32;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) rb.key[i] = kNoRep;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nbw; i += gridDim.x * blockDim.x) {
+    const int rem = n - i * 32;
+    rb.todo[i] = rem >= 32 ? 0xFFFFFFFFu : ((1u << rem) - 1u);
+  }
+}
+
+// One CTA per representative of the chunk: composition test (and the
+// short-word test in word-first order) for every unassigned query; the
+// survivors are queued per class with one global atomic per class and CTA
+// (two passes over the queries: decide into shared memory, then write).
+template <int P>
+__global__ void __launch_bounds__(256) k_serve_filter(DevDB qdb, RepStore rs, RunParams prm, RoundBufs rb, int r0,
+                                                      int word_first) {
+  extern __shared__ uint8_t s_res[];  // per query: 0 = out, 1 + class
+  __shared__ uint32_t s_rc[28], s_cnt[kServeClasses], s_base[kServeClasses], s_pos[kServeClasses];
+  constexpr int A = P == 2 ? 4 : 28;
+  const int r = r0 + blockIdx.x;
+  const uint32_t *rec = rs.words + rs.off[r];
+  if (threadIdx.x < A) s_rc[threadIdx.x] = rec[2 + threadIdx.x];
+  if (threadIdx.x < kServeClasses) s_cnt[threadIdx.x] = s_pos[threadIdx.x] = 0;
+  __syncthreads();
+  const int L1 = (int)rec[0], net1 = (int)rec[1], nb1 = (net1 + 31) / 32;
+  const float s = prm.s;
+  const bool word_here = word_first && !prm.precise && net1 >= 16;
+  const uint32_t *rlist = rs.lists + (int64_t)r * rs.list_words;
+  const int n = qdb.n, nbw = (n + 31) / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int wi = warp; wi < nbw; wi += blockDim.x >> 5) {
+    const uint32_t bits = rb.todo[wi];
+    const int q = wi * 32 + lane;
+    int res = 0;
+    if ((bits >> lane) & 1u) {
+      // a smaller representative of this round may already hold q
+      const bool open = (rb.key[q] >> 32) > (unsigned long long)r;
+      const int L2 = __ldg(qdb.len + q);
+      bool pass = open && !(base_sum<A>(qdb.cnt, q, s_rc) < cutoff_of(L2, s));
+      if (pass && word_here) {
+        const int net2 = __ldg(qdb.net + q);
+        if (net2 >= 16) {
+          const uint32_t *planes = qdb.words + __ldg(qdb.off + q) + qdb.hw;
+          pass = !(word_count<P>(planes, net2, prm.w, rlist) < word_min(L2, prm.w, s));
+        }
+      }
+      if (pass) res = 1 + serve_class(window_of(band_blocks(L1, L2, s), nb1));
+    }
+    if (q < n) s_res[q] = (uint8_t)res;
+    const unsigned pm = __ballot_sync(kFullMask, res != 0);
+    if (res) {
+      const unsigned peers = __match_any_sync(pm, res);
+      if (lane == __ffs(peers) - 1) atomicAdd(&s_cnt[res - 1], (uint32_t)__popc(peers));
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < kServeClasses)
+    s_base[threadIdx.x] = s_cnt[threadIdx.x] ? atomicAdd(&rb.ctl[threadIdx.x], s_cnt[threadIdx.x]) : 0u;
+  __syncthreads();
+  for (int wi = warp; wi < nbw; wi += blockDim.x >> 5) {
+    const int q = wi * 32 + lane;
+    const int res = q < n ? s_res[q] : 0;
+    const unsigned pm = __ballot_sync(kFullMask, res != 0);
+    if (!res) continue;
+    const unsigned peers = __match_any_sync(pm, res);
+    const int leader = __ffs(peers) - 1;
+    uint32_t b = 0;
+    if (lane == leader) b = atomicAdd(&s_pos[res - 1], (uint32_t)__popc(peers));
+    b = __shfl_sync(peers, b, leader);
+    const int64_t slot = (int64_t)s_base[res - 1] + b + __popc(peers & ((1u << lane) - 1u));
+    if (slot < rb.cap) rb.queue[res - 1][slot] = make_int2(r, q);
+  }
+}
+
+// Banded LCS of the queued (representative, query) pairs of one class: the
+// loop of k_align_tiled (align.cu) with the representative taken per pair.
+template <int P, int RING>
+__global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
+    k_serve_align(DevDB qdb, RepStore rs, RunParams prm, RoundBufs rb, int cls, int word_after, uint32_t *scratch,
+                  int64_t scratch_words, uint32_t ring_mask) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ uint32_t s_qn;
+  if (threadIdx.x == 0) s_qn = (int64_t)rb.ctl[cls] < rb.cap ? rb.ctl[cls] : (uint32_t)rb.cap;
+  __syncthreads();
+  const uint32_t qn = s_qn;
+  if (qn == 0) return;
+  typename RingOf<RING>::T ring;
+  if constexpr (RING > 0) {
+    ring.base = smem + threadIdx.x;
+  } else {
+    const int64_t TL = (int64_t)gridDim.x * blockDim.x;
+    if ((int64_t)(ring_mask + 1) * TL > scratch_words) return;  // the host sizes the grid to the scratch
+    ring.base = scratch + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    ring.mask = ring_mask;
+    ring.stride = TL;
+  }
+  const int lane = threadIdx.x & 31;
+  const float s = prm.s;
+  const int hw = qdb.hw;
+  int state = -1;
+  int r = 0, q = 0, i = 0, nq = 0, B = 0, js = 0, je = -1, net1 = 0, nb1 = 0, net2 = 0, L2 = 0, cutoff = 0;
+  int lastcols = 32, frozen = 0, zw = 0;
+  uint32_t vlast = 0;
+  bool active = false;
+  const uint32_t *qpl = nullptr, *rpl = nullptr;
+  uint32_t cur[P], nxt[P];
+  // every loop pass advances a busy lane by one query block or claims:
+  // bounded by the queued pairs' blocks (each at most kMaxBlocks) per warp
+  const long long guard_max = ((long long)qn + 64) * (kMaxBlocks + 4);
+  long long guard = 0;
+  for (;;) {
+    if (++guard > guard_max) {
+      if (lane == 0) atomicExch(&rb.ctl[7], 1u);
+      break;
+    }
+    {  // refill once every lane is idle (lockstep, as in k_align_tiled); the
+       // warp vote runs on all 32 lanes before it is combined per lane
+      const bool any_busy = __any_sync(kFullMask, state >= 0);
+      const bool need = state == -1 && !any_busy;
+      const unsigned nm = __ballot_sync(kFullMask, need);
+      if (nm) {
+        const int leader = __ffs(nm) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&rb.ctl[3 + cls], (uint32_t)__popc(nm));
+        base = __shfl_sync(kFullMask, base, leader);
+        if (need) {
+          const uint32_t idx = base + (uint32_t)__popc(nm & ((1u << lane) - 1u));
+          state = idx < qn ? (int)idx : -2;
+        }
+      }
+    }
+    if (__all_sync(kFullMask, state == -2)) break;
+    bool busy = state >= 0;
+    if (busy && !active) {
+      const int2 e = rb.queue[cls][state];
+      r = e.x;
+      q = e.y;
+      const uint32_t *rrec = rs.words + rs.off[r];
+      const int L1 = (int)rrec[0];
+      net1 = (int)rrec[1];
+      nb1 = (net1 + 31) >> 5;
+      rpl = rrec + hw;
+      vlast = (net1 & 31) ? ((1u << (net1 & 31)) - 1u) : 0xFFFFFFFFu;
+      L2 = __ldg(qdb.len + q);
+      net2 = __ldg(qdb.net + q);
+      nq = (net2 + 31) >> 5;
+      lastcols = (net2 & 31) ? (net2 & 31) : 32;
+      B = band_blocks(L1, L2, s);
+      cutoff = cutoff_of(L2, s);
+      qpl = qdb.words + __ldg(qdb.off + q) + hw;
+      i = 0;
+      js = 0;
+      je = min(B, nb1 - 1);
+      frozen = 0;
+      zw = 0;
+      if ((rb.key[q] >> 32) < (unsigned long long)r) {
+        state = -1;  // a smaller representative already holds q
+        busy = false;
+      } else if (B < 0 || je < 0 || nq == 0) {
+        if (!(0 < cutoff)) atomicMin(&rb.key[q], (unsigned long long)r << 32);
+        state = -1;
+        busy = false;
+      } else {
+        for (int j = 0; j <= je; j++) ring[j] = 0xFFFFFFFFu;
+#pragma unroll
+        for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
+        active = true;
+      }
+    }
+    constexpr int MT = tiled_main(P);
+    const int n = busy ? je - js + 1 : 0;
+    const int full = (int)__reduce_min_sync(kFullMask, busy ? (unsigned)(n / MT) : 0xFFFFFFFFu);
+    int rem = (int)__reduce_max_sync(kFullMask, busy ? (unsigned)(n - MT * full) : 0u);
+    if (!busy) continue;
+    const int cols = (i == nq - 1) ? lastcols : 32;
+    if (i + 1 < nq) {
+#pragma unroll
+      for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
+    }
+    {
+      using Ring = typename RingOf<RING>::T;
+      uint32_t cw = 0, ncw = 0;
+      int base = js;
+      for (int t = 0; t < full; t++, base += MT) {
+        zw += tiled_tile<P, MT, Ring>(ring, rpl, base, je, cols, cur, cw, ncw);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      for (; rem >= MT; rem -= MT, base += MT) {
+        zw += tiled_tile<P, MT, Ring>(ring, rpl, base, je, cols, cur, cw, ncw);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      if (rem > 0) zw += tiled_rem<P, Ring, MT>(rem, ring, rpl, base, je, cols, cur, cw, ncw);
+    }
+    i++;
+    bool finished = i >= nq;
+    if (!finished) {
+      if (i - B > 0) {  // block js leaves the band
+        const uint32_t r0 = ring[js];
+        frozen += __popc(~r0 & (js == nb1 - 1 ? vlast : 0xFFFFFFFFu));
+        zw -= __popc(~r0);
+        js++;
+      }
+      if (i + B <= nb1 - 1) {  // block je enters all-ones
+        je++;
+        ring[je] = 0xFFFFFFFFu;
+      }
+      if (js > je) finished = true;
+    }
+    if (finished) {
+      int sum = frozen;
+      for (int j = js; j <= je; j++) sum += __popc(~ring[j] & (j == nb1 - 1 ? vlast : 0xFFFFFFFFu));
+      bool pass = !(sum < cutoff);
+      if (pass && word_after && net1 >= 16 && net2 >= 16)
+        pass = !(word_count<P>(qpl, net2, prm.w, rs.lists + (int64_t)r * rs.list_words) < word_min(L2, prm.w, s));
+      if (pass) atomicMin(&rb.key[q], ((unsigned long long)r << 32) | (uint32_t)sum);
+      active = false;
+      state = -1;
+      continue;
+    }
+    if (frozen + zw + (net2 - 32 * i) < cutoff) {  // cannot reach the cutoff any more
+      active = false;
+      state = -1;
+      continue;
+    }
+#pragma unroll
+    for (int p = 0; p < P; p++) cur[p] = nxt[p];
+  }
+}
+
+// Drops the queries assigned in this round from the unassigned set and
+// counts the rest.
+__global__ void k_serve_round_end(int n, RoundBufs rb) {
+  const int nbw = (n + 31) / 32;
+  uint32_t left = 0;
+  for (int wi = blockIdx.x * blockDim.x + threadIdx.x; wi < nbw; wi += gridDim.x * blockDim.x) {
+    uint32_t bits = rb.todo[wi];
+    for (uint32_t m = bits; m; m &= m - 1) {
+      const int q = wi * 32 + __ffs(m) - 1;
+      if (rb.key[q] != kNoRep) bits &= ~(1u << (q & 31));
+    }
+    rb.todo[wi] = bits;
+    left += __popc(bits);
+  }
+  for (int o = 16; o; o >>= 1) left += __shfl_xor_sync(kFullMask, left, o);
+  if ((threadIdx.x & 31) == 0 && left) atomicAdd(&rb.ctl[6], left);
+}
+
+using AlignServeFn = void (*)(DevDB, RepStore, RunParams, RoundBufs, int, int, uint32_t *, int64_t, uint32_t);
+
+AlignServeFn serve_align_fn(int type, int cls) {
+  if (type == 0) return cls == 0 ? k_serve_align<2, 64> : cls == 1 ? k_serve_align<2, 128> : k_serve_align<2, 0>;
+  return cls == 0 ? k_serve_align<5, 64> : cls == 1 ? k_serve_align<5, 128> : k_serve_align<5, 0>;
+}
+
+size_t serve_align_smem(int cls) { return cls == 2 ? 0 : (size_t)(cls == 0 ? 64 : 128) * kAlignThreads * 4; }
+
+// NGIA_SERVE_TRACE=1 prints the phases of every batch to stderr.
+bool trace() {
+  static const bool on = [] {
+    const char *t = getenv("NGIA_SERVE_TRACE");
+    return t && *t && *t != '0';
+  }();
+  return on;
+}
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+  int64_t ticket = 0;
+  std::vector<uint32_t> words;
+  std::vector<int64_t> off;
+  int32_t n = 0, longest = 0;
+  std::vector<int32_t> rep, ident;
+  int status = 0;  // 0 waiting or running, 1 done, < 0 error code
+  std::string error;
+  double t_submit = 0, t_start = 0, t_done = 0;
+  int slot = -1, rounds = 0, resident = 0, new_reps = 0;
+};
+
+}  // namespace
+}  // namespace ngia
+
+struct ngia_server;
+
+namespace ngia {
+namespace {
+
+struct Slot {
+  int index = 0;
+  ngia_ctx *ctx = nullptr;
+  RoundBufs rb{};
+  uint32_t *h_ctl = nullptr;                  // pinned
+  unsigned long long *h_key = nullptr;        // pinned, cap_n
+  uint32_t *scratch = nullptr;
+  int64_t scratch_words = 0;
+  int grid[kServeClasses] = {0, 0, 0};
+  std::vector<int32_t> cl, id;
+  std::thread worker;
+};
+
+}  // namespace
+}  // namespace ngia
+
+struct ngia_server {
+  int device = 0, type = 0, num_sms = 0;
+  ngia_params params{};
+  ngia::RunParams prm{};
+  int word_first = 0;
+  ngia_ctx *reps = nullptr;  // the resident representatives' database
+  uint32_t *d_lists = nullptr;
+  ngia::RepStore store{};
+  int64_t cap_n = 0, cap_words = 0;
+  int32_t cap_nb = 0;
+  uint32_t ring_mask = 0;
+  std::vector<std::unique_ptr<ngia::Slot>> slots;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<ngia::Request *> fifo;
+  std::unordered_map<int64_t, std::unique_ptr<ngia::Request>> requests;
+  int64_t next_ticket = 1;
+  bool stop = false;
+};
+
+namespace ngia {
+namespace {
+
+#define CKS(call)                                                                              \
+  do {                                                                                         \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess) return fail(NGIA_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// One batch on one slot.  Returns a status; results land in rq.
+int run_batch(ngia_server *sv, Slot &sl, Request &rq) {
+  ngia_db_view v{};
+  v.n = rq.n;
+  v.type = sv->type;
+  v.longest = rq.longest;
+  v.words = rq.words.data();
+  v.n_words = (int64_t)rq.words.size();
+  v.rec_off = rq.off.data();
+  ngia_ctx *c = sl.ctx;
+  if (trace()) fprintf(stderr, "[serve] slot %d ticket %lld start n=%d\n", sl.index, (long long)rq.ticket, rq.n);
+  int rc = drv::reload_ctx(c, &v);
+  if (rc) return rc;
+  const int n = rq.n, nbw = (n + 31) / 32;
+  cudaStream_t st = c->stream;
+  RoundBufs rb = sl.rb;
+  k_serve_init<<<std::max(1, std::min(c->num_sms, (n + 255) / 256)), 256, 0, st>>>(n, rb);
+  CKS(cudaGetLastError());
+  const int word_after = !sv->word_first && !sv->prm.precise;
+  int r0 = 0, chunk = kFirstChunk;
+  uint32_t left = (uint32_t)n;
+  while (r0 < sv->store.n && left > 0) {
+    const int nr = std::min(chunk, sv->store.n - r0);
+    CKS(cudaMemsetAsync(rb.ctl, 0, 8 * sizeof(uint32_t), st));
+    if (sv->type == 0)
+      k_serve_filter<2><<<nr, 256, (size_t)nbw * 32, st>>>(c->db, sv->store, sv->prm, rb, r0, sv->word_first);
+    else
+      k_serve_filter<5><<<nr, 256, (size_t)nbw * 32, st>>>(c->db, sv->store, sv->prm, rb, r0, sv->word_first);
+    CKS(cudaGetLastError());
+    for (int k = 0; k < kServeClasses; k++) {
+      AlignServeFn fn = serve_align_fn(sv->type, k);
+      DevDB db = c->db;
+      RepStore rs = sv->store;
+      RunParams prm = sv->prm;
+      int cls = k, wa = word_after;
+      uint32_t *scr = sl.scratch;
+      int64_t sw = sl.scratch_words;
+      uint32_t rm = sv->ring_mask;
+      void *args[] = {&db, &rs, &prm, &rb, &cls, &wa, &scr, &sw, &rm};
+      CKS(cudaLaunchKernel((const void *)fn, dim3(sl.grid[k]), dim3(kAlignThreads), args, serve_align_smem(k), st));
+    }
+    k_serve_round_end<<<std::max(1, std::min(c->num_sms, (nbw + 255) / 256)), 256, 0, st>>>(n, rb);
+    CKS(cudaGetLastError());
+    CKS(cudaMemcpyAsync(sl.h_ctl, rb.ctl, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    CKS(cudaStreamSynchronize(st));
+    if (sl.h_ctl[7]) return fail(NGIA_E_DEVICE, "serve: alignment loop bound exceeded (round at rep %d)", r0);
+    if (sl.h_ctl[0] > rb.cap || sl.h_ctl[1] > rb.cap || sl.h_ctl[2] > rb.cap)
+      return fail(NGIA_E_LIMIT, "serve: %u pairs in one round exceed the queue capacity", sl.h_ctl[0]);
+    left = sl.h_ctl[6];
+    if (trace())
+      fprintf(stderr, "[serve] slot %d ticket %lld round %d reps %d..%d pairs %u/%u/%u left %u\n", sl.index,
+              (long long)rq.ticket, rq.rounds, r0, r0 + nr - 1, sl.h_ctl[0], sl.h_ctl[1], sl.h_ctl[2], left);
+    r0 += nr;
+    chunk = std::min(chunk * 2, kMaxChunk);
+    rq.rounds++;
+  }
+  CKS(cudaMemcpyAsync(sl.h_key, rb.key, sizeof(unsigned long long) * (size_t)n, cudaMemcpyDeviceToHost, st));
+  CKS(cudaStreamSynchronize(st));
+  rq.rep.assign(n, 0);
+  rq.ident.assign(n, -1);
+  if (trace()) fprintf(stderr, "[serve] slot %d ticket %lld leftovers %u\n", sl.index, (long long)rq.ticket, left);
+  if (left > 0) {  // greedy clustering of the leftovers
+    rc = drv::begin_subset(c, &sv->params, NGIA_MODE_PLAIN, rb.todo);
+    if (rc) return rc;
+    int32_t done = 0;
+    rc = ngia_cluster_step(c, 0, &done);
+    if (rc) return rc;
+    sl.cl.resize(n);
+    sl.id.resize(n);
+    rc = ngia_cluster_end(c, sl.cl.data(), sl.id.data(), nullptr);
+    if (rc) return rc;
+  }
+  rq.resident = 0;
+  rq.new_reps = 0;
+  for (int q = 0; q < n; q++) {
+    const unsigned long long k = sl.h_key[q];
+    if (k != kNoRep) {
+      rq.rep[q] = (int32_t)(k >> 32);
+      rq.ident[q] = (int32_t)(uint32_t)k;
+      rq.resident++;
+    } else {
+      rq.rep[q] = -1 - sl.cl[q];
+      rq.ident[q] = sl.id[q];
+      if (sl.cl[q] == q) rq.new_reps++;
+    }
+  }
+  return NGIA_OK;
+}
+
+void worker_main(ngia_server *sv, Slot *sl) {
+  cudaSetDevice(sv->device);
+  for (;;) {
+    Request *rq = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(sv->mu);
+      sv->cv_work.wait(lk, [&] { return sv->stop || !sv->fifo.empty(); });
+      if (sv->fifo.empty()) return;  // stopping and nothing left
+      rq = sv->fifo.front();
+      sv->fifo.pop_front();
+      rq->t_start = now_ms();
+      rq->slot = sl->index;
+    }
+    ngia::clear_error();
+    const int rc = run_batch(sv, *sl, *rq);
+    std::string msg;
+    if (rc) {
+      char buf[512];
+      ngia_last_error(buf, sizeof(buf));
+      msg = buf;
+    }
+    {
+      std::lock_guard<std::mutex> lk(sv->mu);
+      rq->t_done = now_ms();
+      rq->status = rc ? rc : 1;
+      rq->error = msg;
+    }
+    sv->cv_done.notify_all();
+  }
+}
+
+void free_slot(Slot &sl) {
+  if (sl.ctx) ngia_close(sl.ctx);
+  for (auto *q : sl.rb.queue) cudaFree(q);
+  cudaFree(sl.rb.ctl);
+  cudaFree(sl.rb.key);
+  cudaFree(sl.rb.todo);
+  cudaFree(sl.scratch);
+  if (sl.h_ctl) cudaFreeHost(sl.h_ctl);
+  if (sl.h_key) cudaFreeHost(sl.h_key);
+  sl = Slot{};
+}
+
+// Device bytes of one slot (context, round buffers, scratch).
+int64_t slot_bytes(const ngia_server *sv, int grid2) {
+  const int A = sv->type ? 28 : 4;
+  const int64_t ctx = 4 * sv->cap_words + sv->cap_n * (8 + 4 + 4 + 4 * A) +
+                      sv->cap_n * (4 + 4 + 4 * ngia::kNumClasses) + (int64_t)sv->cap_n / 8 * 3;
+  const int64_t rounds = (int64_t)kServeClasses * kMaxChunk * sv->cap_n * 8 + sv->cap_n * 8 + sv->cap_n / 8;
+  const int64_t scratch = (int64_t)grid2 * kAlignThreads * (sv->ring_mask + 1) * 4;
+  return ctx + rounds + scratch + (16 << 20);
+}
+
+int open_slot(ngia_server *sv, Slot &sl, int index) {
+  sl.index = index;
+  int rc = drv::open_ctx_capacity(sv->type, sv->cap_n, sv->cap_words, sv->cap_nb, &sl.ctx);
+  if (rc) return rc;
+  const int64_t cap = (int64_t)kMaxChunk * sv->cap_n;
+  for (auto *&q : sl.rb.queue)
+    if (cudaMalloc((void **)&q, sizeof(int2) * (size_t)cap) != cudaSuccess)
+      return fail(NGIA_E_NOMEM, "serve: queue allocation failed");
+  if (cudaMalloc((void **)&sl.rb.ctl, 8 * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMalloc((void **)&sl.rb.key, sizeof(unsigned long long) * (size_t)sv->cap_n) != cudaSuccess ||
+      cudaMalloc((void **)&sl.rb.todo, 4 * (size_t)((sv->cap_n + 31) / 32)) != cudaSuccess ||
+      cudaMallocHost((void **)&sl.h_ctl, 8 * sizeof(uint32_t)) != cudaSuccess ||
+      cudaMallocHost((void **)&sl.h_key, sizeof(unsigned long long) * (size_t)sv->cap_n) != cudaSuccess)
+    return fail(NGIA_E_NOMEM, "serve: slot allocation failed");
+  sl.rb.cap = cap;
+  for (int k = 0; k < kServeClasses; k++) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)serve_align_fn(sv->type, k), kAlignThreads,
+                                                      serve_align_smem(k)) != cudaSuccess ||
+        occ < 1)
+      occ = 1;
+    sl.grid[k] = sv->num_sms * occ;
+  }
+  sl.scratch_words = (int64_t)sl.grid[2] * kAlignThreads * (sv->ring_mask + 1);
+  if (cudaMalloc((void **)&sl.scratch, 4 * (size_t)sl.scratch_words) != cudaSuccess)
+    return fail(NGIA_E_NOMEM, "serve: scratch allocation failed");
+  return NGIA_OK;
+}
+
+void destroy(ngia_server *sv) {
+  {
+    std::lock_guard<std::mutex> lk(sv->mu);
+    sv->stop = true;
+  }
+  sv->cv_work.notify_all();
+  for (auto &sl : sv->slots)
+    if (sl->worker.joinable()) sl->worker.join();
+  for (auto &sl : sv->slots) free_slot(*sl);
+  if (sv->reps) ngia_close(sv->reps);
+  cudaFree(sv->d_lists);
+  delete sv;
+}
+
+// Largest plane-block count of the records of a host view.
+int view_max_blocks(const ngia_db_view *v) {
+  int nb = 0;
+  for (int32_t i = 0; i < v->n; i++) {
+    const int64_t o = v->rec_off[i];
+    if (o < 0 || o + 2 > v->n_words) return INT_MAX;
+    nb = std::max(nb, (int)((v->words[o + 1] + 31) / 32));
+  }
+  return nb;
+}
+
+}  // namespace
+}  // namespace ngia
+
+extern "C" int ngia_serve_open(const ngia_db_view *reps, const ngia_params *params, const ngia_serve_config *cfg,
+                               ngia_server **out) {
+  ngia::clear_error();
+  if (!reps || !params || !out) return fail(NGIA_E_ARG, "ngia_serve_open: null argument");
+  *out = nullptr;
+  int rc = ngia::drv::validate_params(reps->type, params);
+  if (rc) return rc;
+  ngia_serve_config cf = cfg ? *cfg : ngia_serve_config{};
+  if (cf.slots <= 0) cf.slots = 4;
+  if (cf.max_batch <= 0) cf.max_batch = 4096;
+  if (cf.max_record_blocks <= 0) cf.max_record_blocks = 128;
+  if (cf.max_record_blocks > ngia::kMaxBlocks)
+    return fail(NGIA_E_LIMIT, "ngia_serve_open: records of more than %d blocks", ngia::kMaxBlocks);
+  const int hw = reps->type ? 30 : 6, P = reps->type ? 5 : 2;
+  if (cf.max_batch_words <= 0) cf.max_batch_words = (int64_t)cf.max_batch * (hw + P * cf.max_record_blocks);
+  ngia_server *sv = new (std::nothrow) ngia_server();
+  if (!sv) return fail(NGIA_E_NOMEM, "ngia_serve_open: out of host memory");
+  cudaGetDevice(&sv->device);
+  cudaDeviceGetAttribute(&sv->num_sms, cudaDevAttrMultiProcessorCount, sv->device);
+  sv->type = reps->type;
+  sv->params = *params;
+  sv->prm.s = params->similarity;
+  sv->prm.w = params->word_length;
+  sv->prm.precise = params->precise;
+  sv->prm.word_order = 0;
+  sv->prm.refill = 32;
+  sv->word_first = ngia::word_first_of(sv->type, sv->prm);
+  sv->cap_n = cf.max_batch;
+  sv->cap_words = cf.max_batch_words;
+  sv->cap_nb = cf.max_record_blocks;
+  // resident representatives and their k-mer bitsets
+  rc = ngia::drv::open_ctx(reps, true, &sv->reps);
+  if (rc) {
+    ngia::destroy(sv);
+    return rc;
+  }
+  const int bits = sv->type ? 5 : 2;
+  const int lw = std::max(1, (int)((1u << (params->word_length * bits)) / 32u));
+  ngia_ctx *rc_ctx = sv->reps;
+  if (cudaMalloc((void **)&sv->d_lists, 4 * (size_t)lw * (size_t)reps->n) != cudaSuccess) {
+    ngia::destroy(sv);
+    return fail(NGIA_E_NOMEM, "ngia_serve_open: k-mer table allocation failed");
+  }
+  sv->store = ngia::RepStore{rc_ctx->db.words, rc_ctx->db.off, rc_ctx->db.len, rc_ctx->db.net, rc_ctx->db.cnt,
+                             sv->d_lists, rc_ctx->db.n, lw};
+  if (sv->type == 0)
+    ngia::k_rep_lists<2><<<reps->n, 256, 0, rc_ctx->stream>>>(sv->store, params->word_length, sv->d_lists);
+  else
+    ngia::k_rep_lists<5><<<reps->n, 256, 0, rc_ctx->stream>>>(sv->store, params->word_length, sv->d_lists);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(rc_ctx->stream);
+  if (e != cudaSuccess) {
+    ngia::destroy(sv);
+    return fail(NGIA_E_CUDA, "ngia_serve_open: k-mer tables: %s", cudaGetErrorString(e));
+  }
+  uint32_t ring = 1;
+  while ((int)ring < rc_ctx->db.max_nb) ring <<= 1;
+  sv->ring_mask = ring - 1;
+  for (int k = 0; k < 2; k++) {
+    e = cudaFuncSetAttribute((const void *)ngia::serve_align_fn(sv->type, k),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ngia::serve_align_smem(k));
+    if (e != cudaSuccess) {
+      ngia::destroy(sv);
+      return fail(NGIA_E_CUDA, "ngia_serve_open: kernel attributes: %s", cudaGetErrorString(e));
+    }
+  }
+  // slots: as many as asked for and as fit the memory budget
+  size_t free_b = 0, total_b = 0;
+  cudaMemGetInfo(&free_b, &total_b);
+  const int64_t budget = cf.memory_budget > 0 ? cf.memory_budget : (int64_t)(free_b / 2);
+  int occ2 = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, (const void *)ngia::serve_align_fn(sv->type, 2),
+                                                ngia::kAlignThreads, 0);
+  const int64_t per = ngia::slot_bytes(sv, sv->num_sms * std::max(1, occ2));
+  const int n_slots = (int)std::min<int64_t>(cf.slots, budget / per);
+  if (n_slots < 1) {
+    ngia::destroy(sv);
+    return fail(NGIA_E_NOMEM, "ngia_serve_open: one slot needs %lld bytes, the budget is %lld", (long long)per,
+                (long long)budget);
+  }
+  for (int k = 0; k < n_slots; k++) {
+    sv->slots.push_back(std::make_unique<ngia::Slot>());
+    rc = ngia::open_slot(sv, *sv->slots.back(), k);
+    if (rc) {
+      ngia::destroy(sv);
+      return rc;
+    }
+  }
+  for (auto &sl : sv->slots) sl->worker = std::thread(ngia::worker_main, sv, sl.get());
+  *out = sv;
+  return NGIA_OK;
+}
+
+extern "C" int ngia_serve_slots(const ngia_server *s, int32_t *slots) {
+  if (!s || !slots) return fail(NGIA_E_ARG, "ngia_serve_slots: null argument");
+  *slots = (int32_t)s->slots.size();
+  return NGIA_OK;
+}
+
+extern "C" int ngia_serve_submit(ngia_server *s, const ngia_db_view *batch, int64_t *ticket) {
+  ngia::clear_error();
+  if (!s || !batch || !ticket) return fail(NGIA_E_ARG, "ngia_serve_submit: null argument");
+  if (batch->type != s->type) return fail(NGIA_E_ARG, "ngia_serve_submit: batch type %d, service type %d", batch->type,
+                                          s->type);
+  if (batch->n <= 0 || !batch->words || !batch->rec_off || batch->n_words <= 0)
+    return fail(NGIA_E_ARG, "ngia_serve_submit: empty or malformed batch");
+  if (batch->n > s->cap_n || batch->n_words > s->cap_words)
+    return fail(NGIA_E_LIMIT, "ngia_serve_submit: %d records / %lld words exceed a slot (%lld / %lld)", batch->n,
+                (long long)batch->n_words, (long long)s->cap_n, (long long)s->cap_words);
+  const int nb = ngia::view_max_blocks(batch);
+  if (nb > s->cap_nb)
+    return fail(NGIA_E_LIMIT, "ngia_serve_submit: a record of %d blocks exceeds a slot (%d)", nb, s->cap_nb);
+  auto rq = std::make_unique<ngia::Request>();
+  rq->n = batch->n;
+  rq->longest = batch->longest;
+  rq->words.assign(batch->words, batch->words + batch->n_words);
+  rq->off.assign(batch->rec_off, batch->rec_off + batch->n);
+  rq->t_submit = ngia::now_ms();
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stop) return fail(NGIA_E_STATE, "ngia_serve_submit: service is closing");
+    rq->ticket = s->next_ticket++;
+    *ticket = rq->ticket;
+    s->fifo.push_back(rq.get());
+    s->requests.emplace(rq->ticket, std::move(rq));
+  }
+  s->cv_work.notify_one();
+  return NGIA_OK;
+}
+
+extern "C" int ngia_serve_poll(ngia_server *s, int64_t ticket, int32_t wait_ms, int32_t *rep_out,
+                               int32_t *ident_out, ngia_serve_result *res) {
+  ngia::clear_error();
+  if (!s || !res) return fail(NGIA_E_ARG, "ngia_serve_poll: null argument");
+  std::memset(res, 0, sizeof(*res));
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->requests.find(ticket);
+  if (it == s->requests.end()) return fail(NGIA_E_ARG, "ngia_serve_poll: unknown ticket %lld", (long long)ticket);
+  ngia::Request *rq = it->second.get();
+  auto ready = [&] { return rq->status != 0; };
+  if (!ready() && wait_ms != 0) {
+    if (wait_ms < 0)
+      s->cv_done.wait(lk, ready);
+    else
+      s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), ready);
+  }
+  if (!ready()) return NGIA_OK;
+  res->slot = rq->slot;
+  res->rounds = rq->rounds;
+  res->queued_ms = rq->t_start - rq->t_submit;
+  res->run_ms = rq->t_done - rq->t_start;
+  if (rq->status < 0) {
+    const int code = rq->status;
+    const std::string msg = rq->error;
+    s->requests.erase(it);
+    return fail(code, "serve batch %lld: %s", (long long)ticket, msg.c_str());
+  }
+  if (rep_out) std::memcpy(rep_out, rq->rep.data(), sizeof(int32_t) * rq->rep.size());
+  if (ident_out) std::memcpy(ident_out, rq->ident.data(), sizeof(int32_t) * rq->ident.size());
+  res->done = 1;
+  res->resident = rq->resident;
+  res->new_reps = rq->new_reps;
+  s->requests.erase(it);
+  return NGIA_OK;
+}
+
+extern "C" int ngia_serve_close(ngia_server *s) {
+  if (!s) return NGIA_OK;
+  ngia::destroy(s);
+  return NGIA_OK;
+}

@@ -46,6 +46,17 @@ class SynthParams(C.Structure):
                 ("novel_frac", C.c_double), ("seed", C.c_uint64)]
 
 
+class ServeConfig(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("max_batch", C.c_int32), ("max_record_blocks", C.c_int32),
+                ("reserved", C.c_int32), ("max_batch_words", C.c_int64), ("memory_budget", C.c_int64)]
+
+
+class ServeResult(C.Structure):
+    _fields_ = [("done", C.c_int32), ("slot", C.c_int32), ("rounds", C.c_int32), ("resident", C.c_int32),
+                ("new_reps", C.c_int32), ("reserved", C.c_int32), ("queued_ms", C.c_double),
+                ("run_ms", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("iterations", "candidates", "base_pass", "align_pairs", "members",
                                          "band_cells", "filter_bytes", "word_checks", "done_cells")] + \
@@ -103,6 +114,11 @@ def lib() -> C.CDLL:
         "ngia_batch_open": (C.c_int, [P(DBView), I32, P(VP)]),
         "ngia_batch_run": (C.c_int, [VP, P(Params), I32, I64, P(P(I32)), P(P(I32)), P(Stats)]),
         "ngia_batch_close": (C.c_int, [VP]),
+        "ngia_serve_open": (C.c_int, [P(DBView), P(Params), P(ServeConfig), P(VP)]),
+        "ngia_serve_slots": (C.c_int, [VP, P(I32)]),
+        "ngia_serve_submit": (C.c_int, [VP, P(DBView), P(I64)]),
+        "ngia_serve_poll": (C.c_int, [VP, I64, I32, P(I32), P(I32), P(ServeResult)]),
+        "ngia_serve_close": (C.c_int, [VP]),
         "ngia_close": (C.c_int, [VP]),
     }
     for name, (res, args) in sig.items():
@@ -307,6 +323,106 @@ class DB:
         if self._ptr:
             lib().ngia_db_free(self._ptr)
             self._ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Records:
+    """A makeDB-layout database over caller-owned arrays, records in the given
+    order (nothing is re-sorted): e.g. a representative set in creation order,
+    or a slice of a database."""
+
+    def __init__(self, db_type: int, words: np.ndarray, rec_off: np.ndarray):
+        self.type = db_type
+        self.words = np.ascontiguousarray(words, dtype=np.uint32)
+        self.rec_off = np.ascontiguousarray(rec_off, dtype=np.int64)
+        self.n = len(self.rec_off)
+        lens = self.words[self.rec_off] if self.n else np.zeros(1, np.uint32)
+        self.longest, self.shortest = int(lens.max()), int(lens.min())
+        self._view = DBView(self.n, db_type, self.longest, self.shortest,
+                            self.words.ctypes.data_as(C.POINTER(C.c_uint32)), len(self.words), _i64p(self.rec_off))
+
+    @property
+    def view(self) -> DBView:
+        return self._view
+
+    @classmethod
+    def subset(cls, db, idx) -> "Records":
+        """Records idx of db (in that order), copied into one compact array."""
+        hw, P = (6, 2) if db.type == 0 else (30, 5)
+        parts, off, pos = [], [], 0
+        for i in np.asarray(idx, dtype=np.int64):
+            o = int(db.rec_off[i])
+            L = int(db.words[o])
+            rec = db.words[o:o + hw + (L + 31) // 32 * P]
+            parts.append(rec)
+            off.append(pos)
+            pos += len(rec)
+        words = np.concatenate(parts) if parts else np.zeros(1, np.uint32)
+        return cls(db.type, words, np.array(off, dtype=np.int64))
+
+    def close(self) -> None:
+        pass
+
+
+class Server:
+    """Continuous-batching assignment against a resident representative set
+    (ngia_serve_*): submit() queues a batch and returns a ticket, poll()
+    returns (rep, ident, info) once it is done (None before)."""
+
+    def __init__(self, reps, params: Params, slots: int = 4, max_batch: int = 4096, max_record_blocks: int = 128,
+                 memory_budget: int = 0):
+        self.reps = reps
+        cfg = ServeConfig(slots, max_batch, max_record_blocks, 0, 0, memory_budget)
+        self._h = C.c_void_p()
+        _check(lib().ngia_serve_open(C.byref(reps.view), C.byref(params), C.byref(cfg), C.byref(self._h)))
+        self._n = {}
+
+    @property
+    def slots(self) -> int:
+        n = C.c_int32()
+        _check(lib().ngia_serve_slots(self._h, C.byref(n)))
+        return n.value
+
+    def submit(self, batch) -> int:
+        t = C.c_int64()
+        _check(lib().ngia_serve_submit(self._h, C.byref(batch.view), C.byref(t)))
+        self._n[t.value] = batch.n
+        return t.value
+
+    def poll(self, ticket: int, wait_ms: int = 0):
+        n = self._n.get(ticket, 0)  # unknown tickets: the library reports the error
+        rep = np.empty(max(n, 1), dtype=np.int32)
+        ident = np.empty(max(n, 1), dtype=np.int32)
+        res = ServeResult()
+        try:
+            _check(lib().ngia_serve_poll(self._h, ticket, wait_ms, _i32p(rep), _i32p(ident), C.byref(res)))
+        except NgiaError:
+            self._n.pop(ticket, None)
+            raise
+        if not res.done:
+            return None
+        del self._n[ticket]
+        info = {f: getattr(res, f) for f, _ in ServeResult._fields_ if f != "reserved"}
+        return rep[:n], ident[:n], info
+
+    def wait(self, ticket: int):
+        return self.poll(ticket, -1)
+
+    def close(self) -> None:
+        if self._h:
+            lib().ngia_serve_close(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
     def __del__(self):
         try:

@@ -358,6 +358,62 @@ int64_t ora_cluster(const uint32_t *buf, const int64_t *offsets, int n, int type
 }
 
 /* readIndex + readData, func.cu:42-154 (single process: rank 0 of 1). */
+int64_t ora_assign(const uint32_t *rbuf, const int64_t *roff, int nrep, const uint32_t *qbuf,
+                   const int64_t *qoff, int nq, int type, float s, int w, int precise, int nthreads,
+                   int32_t *rep_out, int32_t *ident_out) {
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  uint32_t *lists = (uint32_t *)malloc(sizeof(uint32_t) * 2048 * (size_t)(nrep > 0 ? nrep : 1));
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int r = 0; r < nrep; r++) gen_list(rbuf + roff[r], type, w, lists + (size_t)2048 * r);
+#pragma omp parallel for schedule(dynamic, 4)
+  for (int q = 0; q < nq; q++) {
+    const uint32_t *qr = qbuf + qoff[q];
+    rep_out[q] = INT32_MIN;
+    ident_out[q] = -1;
+    for (int r = 0; r < nrep; r++) {
+      const uint32_t *rr = rbuf + roff[r];
+      if (!base_pass(qr, rr, type, s)) continue;
+      if (!precise && (int)rr[1] >= 16 && (int)qr[1] >= 16 &&
+          !word_pass_thr(word_sum(qr, type, w, lists + (size_t)2048 * r), (int)qr[0], w, s))
+        continue;
+      int band = 0;
+      int64_t cells = 0;
+      const int sum = ora_dp_sum(rr, qr, type, s, &band, &cells);
+      if (!dp_pass(sum, (int)qr[0], s)) continue;
+      rep_out[q] = r;
+      ident_out[q] = sum;
+      break;
+    }
+  }
+  free(lists);
+  int nleft = 0;
+  int64_t *loff = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nq > 0 ? nq : 1));
+  int *lidx = (int *)malloc(sizeof(int) * (size_t)(nq > 0 ? nq : 1));
+  for (int q = 0; q < nq; q++)
+    if (rep_out[q] == INT32_MIN) {
+      loff[nleft] = qoff[q];
+      lidx[nleft++] = q;
+    }
+  int64_t clusters = 0;
+  if (nleft) {
+    int32_t *lc = (int32_t *)malloc(sizeof(int32_t) * (size_t)nleft);
+    int32_t *li = (int32_t *)malloc(sizeof(int32_t) * (size_t)nleft);
+    ora_cluster(qbuf, loff, nleft, type, s, w, precise, nthreads, 0, lc, li, NULL);
+    for (int k = 0; k < nleft; k++) {
+      rep_out[lidx[k]] = -1 - lidx[lc[k]];
+      ident_out[lidx[k]] = li[k];
+      if (lc[k] == k) clusters++;
+    }
+    free(lc);
+    free(li);
+  }
+  free(loff);
+  free(lidx);
+  return clusters;
+}
+
 int ora_load(const char *dir, ora_db *db) {
   memset(db, 0, sizeof(*db));
   char path[4096];

@@ -57,6 +57,21 @@ void ora_pair(const uint32_t *buf, const int64_t *offsets, int type, float s, in
 int ora_dp_sum(const uint32_t *rep, const uint32_t *query, int type, float s,
                int *band, int64_t *cells);
 
+/* Serving (no counterpart in the reference; defined by this project from
+ * the reference's per-pair tests): query q of a batch joins the first
+ * resident representative r (in the order given, i.e. creation order) whose
+ * pair passes the composition test, the short-word test (when precise == 0
+ * and both net lengths are >= 16) and the banded-LCS test of func.cu with r
+ * as the representative; rep_out[q] = r, ident_out[q] = its banded-LCS
+ * score.  Queries no resident representative takes are clustered among
+ * themselves by ora_cluster over the leftover records in batch order:
+ * rep_out[q] = -1 - j where j is the batch index of q's new representative
+ * (j = q for the representative itself, whose ident_out is -1).  Returns
+ * the number of new representatives. */
+int64_t ora_assign(const uint32_t *rbuf, const int64_t *roff, int nrep, const uint32_t *qbuf,
+                   const int64_t *qoff, int nq, int type, float s, int w, int precise, int nthreads,
+                   int32_t *rep_out, int32_t *ident_out);
+
 /* saveResult (func.cu:680-764): writes cluster.txt and represent.fasta. */
 int ora_save(const char *dbdir, const char *outdir, const ora_db *db, const int32_t *cluster,
              int32_t *n_clusters);

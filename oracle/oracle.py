@@ -84,6 +84,25 @@ def pair(words: np.ndarray, rec_off: np.ndarray, db_type: int, s: float, w: int,
     return out
 
 
+def assign(rep_words: np.ndarray, rep_off: np.ndarray, q_words: np.ndarray, q_off: np.ndarray, db_type: int,
+           s: float, w: int, precise: int = 0, threads: int = 0):
+    """Serving semantics (ora_assign): (rep_out, ident_out, new representatives)."""
+    rw = np.ascontiguousarray(rep_words, dtype=np.uint32)
+    ro = np.ascontiguousarray(rep_off, dtype=np.int64)
+    qw = np.ascontiguousarray(q_words, dtype=np.uint32)
+    qo = np.ascontiguousarray(q_off, dtype=np.int64)
+    nq = len(qo)
+    rep = np.empty(nq, dtype=np.int32)
+    ident = np.empty(nq, dtype=np.int32)
+    f = lib().ora_assign
+    f.restype = C.c_int64
+    k = f(rw.ctypes.data_as(C.POINTER(C.c_uint32)), ro.ctypes.data_as(C.POINTER(C.c_int64)), len(ro),
+          qw.ctypes.data_as(C.POINTER(C.c_uint32)), qo.ctypes.data_as(C.POINTER(C.c_int64)), nq, db_type,
+          C.c_float(s), w, precise, threads, rep.ctypes.data_as(C.POINTER(C.c_int32)),
+          ident.ctypes.data_as(C.POINTER(C.c_int32)))
+    return rep, ident, int(k)
+
+
 def dp_sum(rep_rec: np.ndarray, query_rec: np.ndarray, db_type: int, s: float):
     """Alignment score of two raw records; returns (score, band, cells)."""
     r = np.ascontiguousarray(rep_rec, dtype=np.uint32)

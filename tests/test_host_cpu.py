@@ -288,6 +288,38 @@ def test_oracle_stage_counts_are_consistent():
     assert (ident[mem] >= 0).all()
 
 
+def test_oracle_assign_is_first_match_then_greedy():
+    """Serving semantics of the oracle (ora_assign) restated by brute force:
+    each query takes the first resident representative passing all three
+    per-pair tests; the rest are clustered among themselves."""
+    gen = dict(type=0, len_a=600.0, len_b=80.0, len_min=300, len_max=900, subst_max=0.2, indel_max=3,
+               n_ancestors=5)
+    res_seq, res_off = ngia.synth(**gen, n_seqs=150, seed=71)
+    res_db = ngia.DB.pack(0, res_seq, res_off)
+    p = ngia.params_clamp(0, 0.9, 5, 0)
+    cl, _, _ = oracle.cluster(res_db.words, res_db.rec_off, 0, p.similarity, p.word_length, p.precise)
+    reps = ngia.Records.subset(res_db, np.flatnonzero(cl == np.arange(res_db.n)))
+    seq, off = ngia.synth(**gen, n_seqs=210, novel_frac=0.1, seed=71)
+    q = seqs_to_db(0, split(seq, off)[150:])
+    rep, ident, new = oracle.assign(reps.words, reps.rec_off, q.words, q.rec_off, 0, p.similarity, p.word_length,
+                                    p.precise)
+    assert (rep >= 0).sum() > 0 and (rep < 0).sum() > 0
+    words = np.concatenate([reps.words, q.words])
+    offs = np.concatenate([reps.rec_off, q.rec_off + len(reps.words)])
+    for i in range(q.n):
+        exp = None
+        for r in range(reps.n):
+            o = oracle.pair(words, offs, 0, p.similarity, p.word_length, r, reps.n + i)
+            if o[4] and o[5] and o[6]:
+                exp = (r, o[2])
+                break
+        assert (rep[i] < 0) if exp is None else ((rep[i], ident[i]) == exp)
+    left = np.flatnonzero(rep < 0)
+    lc, li, _ = oracle.cluster(q.words, q.rec_off[left], 0, p.similarity, p.word_length, p.precise)
+    assert np.array_equal(rep[left], -1 - left[lc]) and np.array_equal(ident[left], li)
+    assert new == int((lc == np.arange(len(left))).sum())
+
+
 def test_synth_is_deterministic_and_clipped():
     a = ngia.synth(n_seqs=300, n_ancestors=7, seed=9)
     b = ngia.synth(n_seqs=300, n_ancestors=7, seed=9)
