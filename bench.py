@@ -51,9 +51,12 @@ def parse():
     ap.add_argument("--iters-per-step", type=int, default=32)
     ap.add_argument("--similarity", type=float, default=0.85)
     ap.add_argument("--word", type=int, default=5)
-    ap.add_argument("--workload", default="dna_1m", help="dna_small | dna_1m | protein_200k | batch256")
+    ap.add_argument("--workload", default="dna_1m", help="dna_small | dna_1m | protein_200k | batch256 | serve")
     ap.add_argument("--batch-jobs", type=int, default=256)
     ap.add_argument("--batch-max-seqs", type=int, default=200000)
+    ap.add_argument("--serve-batches", type=int, default=200)
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrivals, batches per second")
+    ap.add_argument("--serve-slots", type=int, default=8)
     ap.add_argument("--n-seqs", type=int, default=0, help="override the sequence count (testing only)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--mode", default="graph", choices=["graph", "plain"])
@@ -476,10 +479,155 @@ def run_batch(args, dist: Dist):
     print(json.dumps(out), flush=True)
 
 
+# ---- serving workload ---------------------------------------------------------------
+def serve_workload(args):
+    """Resident representatives: the clustering of the 20,000-sequence DNA
+    configuration (400 ancestors) at the serving similarity.  Batches: sizes
+    log-uniform 1-4,096; each query is a window of log-uniform length
+    200-3,000 over descendants of the same ancestors (10% from novel ones),
+    joined end to end when the window needs more than one.  Arrivals: a
+    Poisson stream of args.serve_rate batches per second."""
+    import math
+
+    import numpy as np
+
+    import ngia
+
+    rng = np.random.default_rng(args.seed)
+    cfg = dict(ngia.CONFIGS["dna_small"])
+    p = ngia.params_clamp(0, args.similarity, args.word, 0)
+    seqs = ngia.synth(**cfg, seed=args.seed)
+    res_db = ngia.DB.pack(0, seqs, seqs.off)
+    seqs.close()
+    with ngia.Context(res_db) as ctx:
+        cl, _, _ = ctx.cluster(p, ngia.MODE_GRAPH)
+    reps = ngia.Records.subset(res_db, np.flatnonzero(cl == np.arange(res_db.n)))
+    sizes = [int(round(math.exp(rng.uniform(0.0, math.log(4096))))) for _ in range(args.serve_batches)]
+    pool_n = sum(sizes) + 64
+    pool = ngia.synth(**{**cfg, "novel_frac": 0.1, "n_seqs": cfg["n_seqs"] + pool_n}, seed=args.seed)
+    desc = [pool.bytes(i) for i in range(cfg["n_seqs"], cfg["n_seqs"] + pool_n)]
+    pool.close()
+    batches, k = [], 0
+    for m in sizes:
+        qs = []
+        for _ in range(m):
+            L = int(round(math.exp(rng.uniform(math.log(200), math.log(3000)))))
+            buf = desc[k % len(desc)]
+            j = k + 1
+            while len(buf) < L:
+                buf += desc[j % len(desc)]
+                j += 1
+            k += 1
+            a = int(rng.integers(0, len(buf) - L + 1))
+            qs.append(buf[a:a + L])
+        off = np.zeros(len(qs) + 1, dtype=np.int64)
+        off[1:] = np.cumsum([len(q) for q in qs])
+        batches.append(ngia.DB.pack(0, b"".join(qs), off))
+    gaps = rng.exponential(1.0 / args.serve_rate, size=len(batches))
+    return p, res_db, reps, batches, np.cumsum(gaps) - gaps[0]
+
+
+def run_serve(args, dist: Dist):
+    """Serving arm: the batches are submitted at their Poisson arrival times
+    by one thread while another collects them; latency = arrival to result
+    (queueing included), throughput = queries / (first arrival to last
+    result).  A bounded sample of the batches is replayed by the oracle."""
+    import threading as th
+
+    import numpy as np
+
+    import ngia
+
+    if dist.rank != 0:
+        return
+    t0 = time.perf_counter()
+    p, res_db, reps, batches, arrive = serve_workload(args)
+    t_gen = time.perf_counter() - t0
+    srv = ngia.Server(reps, p, slots=args.serve_slots, max_batch=4096, max_record_blocks=96)
+    for b in batches[:args.warmup]:
+        srv.wait(srv.submit(b))
+    tickets = [None] * len(batches)
+    t_sub = [0.0] * len(batches)
+    ready = th.Semaphore(0)
+
+    def submitter(start):
+        for i, b in enumerate(batches):
+            delay = start + arrive[i] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            t_sub[i] = time.perf_counter()
+            tickets[i] = srv.submit(b)
+            ready.release()
+
+    clocks = Clocks(dist.local)
+    clocks.start()
+    start = time.perf_counter() + 0.05
+    sub = th.Thread(target=submitter, args=(start,))
+    sub.start()
+    results, t_done = [None] * len(batches), [0.0] * len(batches)
+    for i in range(len(batches)):
+        ready.acquire()
+        results[i] = srv.wait(tickets[i])
+        t_done[i] = t_sub[i] + (results[i][2]["queued_ms"] + results[i][2]["run_ms"]) / 1e3
+    sub.join()
+    clk = clocks.stop()
+    end = max(t_done)
+    # capacity: every batch submitted at once (the slots stay busy)
+    t_sat = time.perf_counter()
+    sat_t = [srv.submit(b) for b in batches]
+    sat = [srv.wait(t) for t in sat_t]
+    T_sat = time.perf_counter() - t_sat
+    same_runs = all(np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) for a, b in zip(results, sat))
+    lat = np.array([(t_done[i] - (start + arrive[i])) * 1e3 for i in range(len(batches))])
+    run_ms = np.array([r[2]["run_ms"] for r in results])
+    n_q = sum(b.n for b in batches)
+    T = end - start
+    # oracle replay of a bounded sample (the smallest batches first)
+    from oracle import oracle
+    checked, same, t_chk = 0, True, time.perf_counter()
+    for i in np.argsort([b.n for b in batches]):
+        if time.perf_counter() - t_chk > args.cpu_seconds:
+            break
+        b = batches[i]
+        rep, ident, _ = oracle.assign(reps.words, reps.rec_off, b.words, b.rec_off, 0, p.similarity, p.word_length,
+                                      p.precise)
+        same = same and np.array_equal(rep, results[i][0]) and np.array_equal(ident, results[i][1])
+        checked += 1
+    slots = srv.slots
+    srv.close()
+    out = {"metric": "seqs/sec (queries served: assigned to resident representatives or clustered, bit-exact)",
+           "value": n_q / T, "unit": "query seqs/s", "n_gpus": 1, "steps": len(batches), "warmup": args.warmup,
+           "ms_per_step": 1e3 * T / len(batches), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "u32", "data": "synthetic (seeded generators with the configuration's shapes)",
+           "config": {"workload": f"serve: resident representatives of the 20,000-sequence DNA configuration at "
+                                  f"s={p.similarity:.2f} ({reps.n:,} representatives), {len(batches)} batches of "
+                                  f"log-uniform 1-4,096 DNA queries (lengths log-uniform 200-3,000, same ancestors "
+                                  f"plus 10% novel), Poisson arrivals at {args.serve_rate:g} batches/s",
+                      "slots": slots, "queries": n_q, "generation_s": round(t_gen, 1)},
+           "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                          "mean": float(lat.mean()), "max": float(lat.max()),
+                          "run_p50": float(np.percentile(run_ms, 50)), "run_p99": float(np.percentile(run_ms, 99))},
+           "offered_batches_per_s": args.serve_rate, "achieved_batches_per_s": len(batches) / T,
+           "gcups": sum(r[2]["cells"] for r in results) / T / 1e9,
+           "pairs_aligned": int(sum(r[2]["pairs"] for r in results)),
+           "capacity": {"queries_per_s": n_q / T_sat, "batches_per_s": len(batches) / T_sat,
+                        "gcups": sum(r[2]["cells"] for r in sat) / T_sat / 1e9,
+                        "form": "all batches submitted at once"},
+           "identical_open_loop_and_saturated": bool(same_runs),
+           "oracle_replay": {"batches": checked, "queries": int(sum(batches[i].n for i in
+                                                                   np.argsort([b.n for b in batches])[:checked])),
+                             "identical": bool(same)},
+           "clocks": clk}
+    print(json.dumps(out), flush=True)
+    for b in batches:
+        b.close()
+    res_db.close()
+
+
 def main():
     args = parse()
-    if args.workload.startswith("batch"):
-        # one hardware queue per job stream (the default is 8)
+    if args.workload.startswith("batch") or args.workload == "serve":
+        # one hardware queue per job / slot stream (the default is 8)
         os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     dist = Dist()
     try:
@@ -489,6 +637,8 @@ def main():
             run_reference(args, dist)
         elif args.workload.startswith("batch"):
             run_batch(args, dist)
+        elif args.workload == "serve":
+            run_serve(args, dist)
         else:
             run_ours(args, dist)
     finally:

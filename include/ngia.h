@@ -258,6 +258,8 @@ typedef struct ngia_serve_result {
     int32_t reserved;
     double  queued_ms;   /* submit -> start on a slot                           */
     double  run_ms;      /* start on a slot -> finished                         */
+    int64_t pairs;       /* (representative, query) pairs aligned in assignment */
+    int64_t cells;       /* in-band cells those alignments computed             */
 } ngia_serve_result;
 
 /* Opens the service on the current device; params are clamped

@@ -177,11 +177,13 @@ __device__ __forceinline__ void flush_align_stats(RunState *st, unsigned long lo
 }
 
 template <int P, int WC>
-__global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_win(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode) {
+__global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
+    k_align_win(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode, int warp_pairs) {
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
   AlignHdr h;
   if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
+  if (h.qn <= warp_pairs) return;  // few pairs: k_align_warp takes them
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
   RunState *st = rb.st;
@@ -344,11 +346,12 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC)) k_align_
 //
 template <int P, int RING>
 __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
-    k_align_tiled(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode) {
+    k_align_tiled(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode, int warp_pairs) {
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
   AlignHdr h;
   if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
+  if (h.qn <= warp_pairs) return;  // few pairs: k_align_warp takes them
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
   RunState *st = rb.st;
@@ -485,8 +488,133 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 }
 
 
+// ---- one warp per pair ------------------------------------------------------------
+// For iterations with few queued pairs of a class, the latency of one pair
+// on one thread (every residue of the query against the whole band window,
+// in order) bounds the iteration.  k_align_warp gives each pair a warp.  The
+// band's rows are cut into strips of 32, one row word per lane, and all 32
+// lanes apply the same query residue together: the strip is one 1,024-bit
+// addition row + (row & match) + carry, whose word carries are resolved with
+// carry lookahead over the lanes — lane l's word sum yields a generate bit
+// (it overflowed) and a propagate bit (it is all ones); with G and Pm the
+// ballots of those, the carry into every lane is a bit of
+// ((G | Pm) + G + carry_in) ^ (G | Pm) ^ G, and that 32-bit addition's own
+// carry is the strip's carry out.  Strips of a query block run bottom-up, the
+// column carries of one strip (a 32-bit mask) feeding the next; the lowest
+// band row takes carry 0 and the top row's carry is dropped (the reference's
+// band semantics).  Band rows live in shared memory (all nb1 rows of the
+// pair, all-ones until they enter the band), loaded at a strip's start and
+// stored at its end; after every query block the zero count (kept as the
+// sum of the lanes' row changes) gives the exact early rejection test.
+template <int P>
+__global__ void __launch_bounds__(kAlignThreads)
+    k_align_warp(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode, int warp_pairs) {
+  extern __shared__ __align__(16) uint32_t smem[];
+  __shared__ uint64_t bar;
+  AlignHdr h;
+  if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
+  if (h.qn > warp_pairs) return;  // many pairs: the thread-per-pair kernel takes them
+  const uint32_t *s_pl = smem;
+  const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint32_t *rows = smem + (((db.max_nb * P + 3) & ~3) + kListWords) + warp * db.max_nb;
+  RunState *st = rb.st;
+  const float s = prm.s;
+  const int nb1 = h.nb1;
+  const uint32_t vlast = (h.net1 & 31) ? ((1u << (h.net1 & 31)) - 1u) : 0xFFFFFFFFu;
+  unsigned long long n_pairs = 0, n_members = 0, n_cells = 0, n_done = 0;
+  const int nwarps = gridDim.x * (blockDim.x >> 5);
+  for (int e = blockIdx.x * (blockDim.x >> 5) + warp; e < h.qn; e += nwarps) {
+    const int entry = score_mode ? e : rb.queue[cls][e];
+    const int cand = score_mode ? rb.score_cands[entry] : entry;
+    const int L2 = __ldg(db.len + cand), net2 = __ldg(db.net + cand);
+    const int nq = (net2 + 31) >> 5;
+    const int lastcols = (net2 & 31) ? (net2 & 31) : 32;
+    const int B = band_blocks(h.L1, L2, s);
+    const int cutoff = cutoff_of(L2, s);
+    const uint32_t *qpl = db.words + __ldg(db.off + cand) + db.hw;
+    if (!score_mode && lane == 0) {
+      n_pairs++;
+      n_cells += (unsigned long long)band_cells(B, nb1, net2);
+    }
+    if (B < 0 || nq == 0) {
+      if (lane == 0) finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, 0, cutoff, L2, net2, qpl, s_list, n_members);
+      continue;
+    }
+    for (int j = lane; j < nb1; j += 32) rows[j] = 0xFFFFFFFFu;
+    __syncwarp();
+    int delta = 0;
+    bool rejected = false;
+    uint32_t nxt[P];
+#pragma unroll
+    for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + p);
+    for (int i = 0; i < nq; i++) {
+      uint32_t cur[P];
+#pragma unroll
+      for (int p = 0; p < P; p++) {
+        cur[p] = nxt[p];
+        if (i + 1 < nq) nxt[p] = __ldg(qpl + (i + 1) * P + p);
+      }
+      const int js = max(i - B, 0), je = min(i + B, nb1 - 1);
+      const int strips = je >= js ? (je - js + 32) >> 5 : 0;
+      const int cols = (i == nq - 1) ? lastcols : 32;
+      if (!score_mode && lane == 0) n_done += (unsigned long long)(je - js + 1) * cols;
+      uint32_t cmask = 0;  // carry into the strip, bit k for column k
+      for (int sidx = 0; sidx < strips; sidx++) {
+        const int j = js + 32 * sidx + lane;
+        const bool have = j <= je;
+        uint32_t row = have ? rows[j] : 0u, pl[P];
+#pragma unroll
+        for (int p = 0; p < P; p++) pl[p] = have ? s_pl[j * P + p] : 0u;
+        const uint32_t row0 = row;
+        uint32_t cout = 0;
+        for (int k = 0; k < cols; k++) {
+          uint32_t x = row;
+#pragma unroll
+          for (int p = 0; p < P; p++) x &= ~(pl[p] ^ (0u - ((cur[p] >> k) & 1u)));
+          uint32_t sum, gen;
+          asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(sum), "=r"(gen) : "r"(row), "r"(x));
+          const uint32_t G = __ballot_sync(kFullMask, have && gen);
+          const uint32_t Pm = __ballot_sync(kFullMask, have && sum == 0xFFFFFFFFu);
+          const uint32_t X = G | Pm;
+          const unsigned long long tot = (unsigned long long)X + G + ((cmask >> k) & 1u);
+          cout |= (uint32_t)(tot >> 32) << k;
+          const uint32_t c = (((uint32_t)tot ^ X ^ G) >> lane) & 1u;
+          if (have) row = (sum + c) | (row ^ x);
+        }
+        if (have) {
+          rows[j] = row;
+          const uint32_t m = (j == nb1 - 1) ? vlast : 0xFFFFFFFFu;
+          delta += __popc(~row & m) - __popc(~row0 & m);
+        }
+        cmask = cout;
+      }
+      __syncwarp();  // this block's rows are stored before the next block loads them
+      if (!score_mode && i + 1 < nq) {
+        int z = delta;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(kFullMask, z, o);
+        if (z + (net2 - 32 * (i + 1)) < cutoff) {  // cannot reach the cutoff any more
+          rejected = true;
+          break;
+        }
+      }
+    }
+    if (rejected) continue;
+    int sum = delta;
+#pragma unroll
+    for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFullMask, sum, o);
+    if (lane == 0) finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, sum, cutoff, L2, net2, qpl, s_list, n_members);
+    __syncwarp();
+  }
+  flush_align_stats(st, n_pairs, n_members, n_cells, n_done);
+}
+
 // ---- dispatch ---------------------------------------------------------------------
-typedef void (*AlignFn)(DevDB, RunBufs, RunParams, int, int);
+typedef void (*AlignFn)(DevDB, RunBufs, RunParams, int, int, int);
+
+static AlignFn warp_fn(int type) { return type == 0 ? k_align_warp<2> : k_align_warp<5>; }
+constexpr int kWarpKernel = kNumClasses;  // index of the warp kernel in the attribute table
 
 static AlignFn align_fn(int type, int cls) {
   if (type == 0) {
@@ -509,10 +637,12 @@ static AlignFn align_fn(int type, int cls) {
   }
 }
 
-// Dynamic shared memory: rep planes | k-mer bitset | (tiled class) row ring.
+// Dynamic shared memory: rep planes | k-mer bitset | (tiled class) row ring
+// | (warp kernel, cls = kWarpKernel) every row of one pair per warp.
 static size_t align_smem(int type, int max_nb, int cls) {
   const int P = type ? 5 : 2;
   size_t words = (size_t)(((max_nb * P + 3) & ~3) + kListWords);
+  if (cls == kWarpKernel) return 4u * (words + (size_t)(kAlignThreads / 32) * max_nb);
   if (is_tiled_class(type, cls)) words += (size_t)class_cap(type, cls) * kAlignThreads;
   return 4u * words;
 }
@@ -523,17 +653,19 @@ static size_t align_smem(int type, int max_nb, int cls) {
 // longer ones.
 cudaError_t align_configure(int type, int max_nb) {
   static std::mutex mu;
-  static int configured[64][2][kNumClasses] = {};
+  static int configured[64][2][kNumClasses + 1] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(mu);
-  for (int c = 0; c < num_classes(type); c++) {
+  for (int c = 0; c <= kNumClasses; c++) {
+    if (c >= num_classes(type) && c != kWarpKernel) continue;
     const int want = (int)align_smem(type, max_nb, c);
     int &have = configured[dev][type ? 1 : 0][c];
     if (want <= have) continue;
-    e = cudaFuncSetAttribute((const void *)align_fn(type, c), cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+    const void *fn = c == kWarpKernel ? (const void *)warp_fn(type) : (const void *)align_fn(type, c);
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
     if (e != cudaSuccess) return e;
     have = want;
   }
@@ -541,24 +673,33 @@ cudaError_t align_configure(int type, int max_nb) {
 }
 
 // Resident CTAs per SM of class `cls` (persistent grid = that x SM count).
+// (cls = kNumClasses: the warp kernel.)
 int align_occupancy(int type, int cls, int max_nb) {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)align_fn(type, cls), kAlignThreads,
-                                                    align_smem(type, max_nb, cls)) != cudaSuccess)
+  const void *fn = cls == kWarpKernel ? (const void *)warp_fn(type) : (const void *)align_fn(type, cls);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kAlignThreads, align_smem(type, max_nb, cls)) !=
+      cudaSuccess)
     return 1;
   return nb < 1 ? 1 : nb;
 }
 
 int align_threads() { return kAlignThreads; }
 
+// Launches class `cls`: the thread-per-pair kernel, and (in clustering) the
+// warp-per-pair kernel; which of the two works is decided on the device from
+// the class's queued pair count against c->warp_pairs.
 cudaError_t launch_align(ngia_ctx *c, int cls, cudaStream_t s, int score_mode) {
   AlignFn fn = align_fn(c->db.type, cls);
-  const size_t smem = align_smem(c->db.type, c->db.max_nb, cls);
   DevDB db = c->db;
   RunBufs rb = c->rb;
   RunParams prm = c->prm;
-  void *args[] = {&db, &rb, &prm, &cls, &score_mode};
-  return cudaLaunchKernel((const void *)fn, dim3(c->grid_align[cls]), dim3(kAlignThreads), args, smem, s);
+  int wp = score_mode ? -1 : c->warp_pairs;
+  void *args[] = {&db, &rb, &prm, &cls, &score_mode, &wp};
+  cudaError_t e = cudaLaunchKernel((const void *)fn, dim3(c->grid_align[cls]), dim3(kAlignThreads), args,
+                                   align_smem(c->db.type, c->db.max_nb, cls), s);
+  if (e != cudaSuccess || wp < 0) return e;
+  return cudaLaunchKernel((const void *)warp_fn(c->db.type), dim3(c->grid_warp), dim3(kAlignThreads), args,
+                          align_smem(c->db.type, c->db.max_nb, kWarpKernel), s);
 }
 
 

@@ -255,6 +255,12 @@ void size_grids(ngia_ctx *c, bool by_size) {
   for (int k = 0; k < ngia::num_classes(type); k++)
     c->grid_align[k] = c->num_sms * ngia::align_occupancy(type, k, c->cap_nb);
   c->grid_filter = c->num_sms * 8;
+  // warp-per-pair: the whole GPU's warps; a class goes warp-per-pair when it
+  // has at most two pairs per warp (the pair latency on one thread is ~20x
+  // that on a warp, at ~3x the instructions per cell)
+  c->grid_warp = c->num_sms * ngia::align_occupancy(type, ngia::kNumClasses, c->cap_nb);
+  c->warp_pairs = 2 * c->grid_warp * (ngia::align_threads() / 32);
+  if (const char *w = getenv("NGIA_WARP_PAIRS")) c->warp_pairs = atoi(w);
   if (by_size) {
     const int64_t n = std::max(1, c->db.n), nbw = (n + 31) / 32;
     const int by_n = (int)std::min<int64_t>((n + 127) / 128, INT32_MAX);

@@ -33,6 +33,8 @@ struct ngia_ctx {
   // launch shapes
   int grid_filter = 0;
   int grid_align[ngia::kNumClasses] = {0};
+  int grid_warp = 0;    // CTAs of the warp-per-pair kernel
+  int warp_pairs = -1;  // a class with at most this many pairs runs warp-per-pair
   // graph form of the greedy loop
   cudaGraphExec_t graph_exec = nullptr;
   cudaGraph_t graph = nullptr;

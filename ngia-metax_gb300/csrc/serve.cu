@@ -11,7 +11,7 @@
 // One batch runs on one slot — a context of fixed capacity with its own
 // stream, driven by its own host thread:
 //  1. assignment, in rounds over chunks of representatives in creation order
-//     (64, 128, then 256 at a time): k_serve_filter tests every unassigned
+//     (64, 128, ... doubling up to 1,024): k_serve_filter tests every unassigned
 //     query against every representative of the chunk (composition, and the
 //     short-word test when it goes first) and queues the surviving pairs by
 //     band-window width; k_serve_align runs the banded LCS of each pair with
@@ -54,7 +54,7 @@ namespace {
 
 constexpr int kServeClasses = 3;    // band windows <= 64 blocks, <= 128, wider
 constexpr int kFirstChunk = 64;     // representatives in the first round
-constexpr int kMaxChunk = 256;      // ... doubling up to this many per round
+constexpr int kMaxChunk = 1024;     // ... doubling up to this many per round
 constexpr unsigned long long kNoRep = ~0ull;
 
 // Device view of the resident representatives.
@@ -73,6 +73,7 @@ struct RoundBufs {
   uint32_t *ctl;               // [0..2] pairs queued per class, [3..5] claimed, [6] queries left
   unsigned long long *key;     // per query: rep << 32 | score of the best accepting rep
   uint32_t *todo;              // bitmap of the queries not assigned yet
+  unsigned long long *stats;   // [0] pairs aligned, [1] in-band cells computed
   int64_t cap;                 // pairs per class queue
 };
 
@@ -105,6 +106,7 @@ __global__ void k_rep_lists(RepStore rs, int w, uint32_t *lists) {
 
 __global__ void k_serve_init(int n, RoundBufs rb) {
   const int nbw = (n + 31) / 32;
+  if (blockIdx.x == 0 && threadIdx.x < 2) rb.stats[threadIdx.x] = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) rb.key[i] = kNoRep;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nbw; i += gridDim.x * blockDim.x) {
     const int rem = n - i * 32;
@@ -209,6 +211,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
   bool active = false;
   const uint32_t *qpl = nullptr, *rpl = nullptr;
   uint32_t cur[P], nxt[P];
+  unsigned long long n_pairs = 0, n_cells = 0;
   // every loop pass advances a busy lane by one query block or claims:
   // bounded by the queued pairs' blocks (each at most kMaxBlocks) per warp
   const long long guard_max = ((long long)qn + 64) * (kMaxBlocks + 4);
@@ -270,6 +273,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 #pragma unroll
         for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
         active = true;
+        n_pairs++;
       }
     }
     constexpr int MT = tiled_main(P);
@@ -278,6 +282,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
     int rem = (int)__reduce_max_sync(kFullMask, busy ? (unsigned)(n - MT * full) : 0u);
     if (!busy) continue;
     const int cols = (i == nq - 1) ? lastcols : 32;
+    n_cells += (unsigned long long)n * cols * 32;
     if (i + 1 < nq) {
 #pragma unroll
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
@@ -332,6 +337,14 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 #pragma unroll
     for (int p = 0; p < P; p++) cur[p] = nxt[p];
   }
+  for (int o = 16; o; o >>= 1) {
+    n_pairs += __shfl_down_sync(kFullMask, n_pairs, o);
+    n_cells += __shfl_down_sync(kFullMask, n_cells, o);
+  }
+  if (lane == 0 && n_pairs) {
+    atomicAdd(&rb.stats[0], n_pairs);
+    atomicAdd(&rb.stats[1], n_cells);
+  }
 }
 
 // Drops the queries assigned in this round from the unassigned set and
@@ -370,6 +383,15 @@ bool trace() {
   return on;
 }
 
+// Driver of the leftover clustering: NGIA_SERVE_LEFTOVERS=plain|graph.
+int leftover_mode() {
+  static const int m = [] {
+    const char *t = getenv("NGIA_SERVE_LEFTOVERS");
+    return t && std::strcmp(t, "plain") == 0 ? NGIA_MODE_PLAIN : NGIA_MODE_GRAPH;
+  }();
+  return m;
+}
+
 double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
 }
@@ -384,6 +406,7 @@ struct Request {
   std::string error;
   double t_submit = 0, t_start = 0, t_done = 0;
   int slot = -1, rounds = 0, resident = 0, new_reps = 0;
+  int64_t pairs = 0, cells = 0;
 };
 
 }  // namespace
@@ -400,6 +423,7 @@ struct Slot {
   RoundBufs rb{};
   uint32_t *h_ctl = nullptr;                  // pinned
   unsigned long long *h_key = nullptr;        // pinned, cap_n
+  unsigned long long *h_stats = nullptr;      // pinned, 2
   uint32_t *scratch = nullptr;
   int64_t scratch_words = 0;
   int grid[kServeClasses] = {0, 0, 0};
@@ -460,14 +484,19 @@ int run_batch(ngia_server *sv, Slot &sl, Request &rq) {
   const int word_after = !sv->word_first && !sv->prm.precise;
   int r0 = 0, chunk = kFirstChunk;
   uint32_t left = (uint32_t)n;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  if (trace())
+    for (auto &e : ev) cudaEventCreate(&e);
   while (r0 < sv->store.n && left > 0) {
     const int nr = std::min(chunk, sv->store.n - r0);
     CKS(cudaMemsetAsync(rb.ctl, 0, 8 * sizeof(uint32_t), st));
+    if (ev[0]) cudaEventRecord(ev[0], st);
     if (sv->type == 0)
       k_serve_filter<2><<<nr, 256, (size_t)nbw * 32, st>>>(c->db, sv->store, sv->prm, rb, r0, sv->word_first);
     else
       k_serve_filter<5><<<nr, 256, (size_t)nbw * 32, st>>>(c->db, sv->store, sv->prm, rb, r0, sv->word_first);
     CKS(cudaGetLastError());
+    if (ev[1]) cudaEventRecord(ev[1], st);
     for (int k = 0; k < kServeClasses; k++) {
       AlignServeFn fn = serve_align_fn(sv->type, k);
       DevDB db = c->db;
@@ -480,36 +509,59 @@ int run_batch(ngia_server *sv, Slot &sl, Request &rq) {
       void *args[] = {&db, &rs, &prm, &rb, &cls, &wa, &scr, &sw, &rm};
       CKS(cudaLaunchKernel((const void *)fn, dim3(sl.grid[k]), dim3(kAlignThreads), args, serve_align_smem(k), st));
     }
+    if (ev[2]) cudaEventRecord(ev[2], st);
     k_serve_round_end<<<std::max(1, std::min(c->num_sms, (nbw + 255) / 256)), 256, 0, st>>>(n, rb);
     CKS(cudaGetLastError());
+    if (ev[3]) cudaEventRecord(ev[3], st);
     CKS(cudaMemcpyAsync(sl.h_ctl, rb.ctl, 8 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
     CKS(cudaStreamSynchronize(st));
     if (sl.h_ctl[7]) return fail(NGIA_E_DEVICE, "serve: alignment loop bound exceeded (round at rep %d)", r0);
     if (sl.h_ctl[0] > rb.cap || sl.h_ctl[1] > rb.cap || sl.h_ctl[2] > rb.cap)
       return fail(NGIA_E_LIMIT, "serve: %u pairs in one round exceed the queue capacity", sl.h_ctl[0]);
     left = sl.h_ctl[6];
-    if (trace())
-      fprintf(stderr, "[serve] slot %d ticket %lld round %d reps %d..%d pairs %u/%u/%u left %u\n", sl.index,
-              (long long)rq.ticket, rq.rounds, r0, r0 + nr - 1, sl.h_ctl[0], sl.h_ctl[1], sl.h_ctl[2], left);
+    if (trace()) {
+      float f = 0, a = 0, e = 0;
+      cudaEventElapsedTime(&f, ev[0], ev[1]);
+      cudaEventElapsedTime(&a, ev[1], ev[2]);
+      cudaEventElapsedTime(&e, ev[2], ev[3]);
+      fprintf(stderr,
+              "[serve] slot %d ticket %lld round %d reps %d..%d pairs %u/%u/%u left %u  filter %.3f align %.3f end "
+              "%.3f ms\n",
+              sl.index, (long long)rq.ticket, rq.rounds, r0, r0 + nr - 1, sl.h_ctl[0], sl.h_ctl[1], sl.h_ctl[2], left,
+              f, a, e);
+    }
     r0 += nr;
     chunk = std::min(chunk * 2, kMaxChunk);
     rq.rounds++;
   }
+  for (auto &e : ev)
+    if (e) cudaEventDestroy(e);
   CKS(cudaMemcpyAsync(sl.h_key, rb.key, sizeof(unsigned long long) * (size_t)n, cudaMemcpyDeviceToHost, st));
+  CKS(cudaMemcpyAsync(sl.h_stats, rb.stats, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
   CKS(cudaStreamSynchronize(st));
+  rq.pairs = (int64_t)sl.h_stats[0];
+  rq.cells = (int64_t)sl.h_stats[1];
   rq.rep.assign(n, 0);
   rq.ident.assign(n, -1);
   if (trace()) fprintf(stderr, "[serve] slot %d ticket %lld leftovers %u\n", sl.index, (long long)rq.ticket, left);
   if (left > 0) {  // greedy clustering of the leftovers
-    rc = drv::begin_subset(c, &sv->params, NGIA_MODE_PLAIN, rb.todo);
+    const double t0 = now_ms();
+    const int mode = leftover_mode();
+    rc = drv::begin_subset(c, &sv->params, mode, rb.todo);
     if (rc) return rc;
+    const double t1 = now_ms();
     int32_t done = 0;
     rc = ngia_cluster_step(c, 0, &done);
     if (rc) return rc;
     sl.cl.resize(n);
     sl.id.resize(n);
-    rc = ngia_cluster_end(c, sl.cl.data(), sl.id.data(), nullptr);
+    ngia_stats gst;
+    rc = ngia_cluster_end(c, sl.cl.data(), sl.id.data(), &gst);
     if (rc) return rc;
+    if (trace())
+      fprintf(stderr, "[serve] slot %d ticket %lld greedy %s: %lld iterations, begin %.2f ms, loop %.2f ms\n",
+              sl.index, (long long)rq.ticket, mode == NGIA_MODE_GRAPH ? "graph" : "plain", (long long)gst.iterations,
+              t1 - t0, now_ms() - t1);
   }
   rq.resident = 0;
   rq.new_reps = 0;
@@ -565,6 +617,8 @@ void free_slot(Slot &sl) {
   cudaFree(sl.rb.ctl);
   cudaFree(sl.rb.key);
   cudaFree(sl.rb.todo);
+  cudaFree(sl.rb.stats);
+  if (sl.h_stats) cudaFreeHost(sl.h_stats);
   cudaFree(sl.scratch);
   if (sl.h_ctl) cudaFreeHost(sl.h_ctl);
   if (sl.h_key) cudaFreeHost(sl.h_key);
@@ -593,7 +647,9 @@ int open_slot(ngia_server *sv, Slot &sl, int index) {
       cudaMalloc((void **)&sl.rb.key, sizeof(unsigned long long) * (size_t)sv->cap_n) != cudaSuccess ||
       cudaMalloc((void **)&sl.rb.todo, 4 * (size_t)((sv->cap_n + 31) / 32)) != cudaSuccess ||
       cudaMallocHost((void **)&sl.h_ctl, 8 * sizeof(uint32_t)) != cudaSuccess ||
-      cudaMallocHost((void **)&sl.h_key, sizeof(unsigned long long) * (size_t)sv->cap_n) != cudaSuccess)
+      cudaMallocHost((void **)&sl.h_key, sizeof(unsigned long long) * (size_t)sv->cap_n) != cudaSuccess ||
+      cudaMalloc((void **)&sl.rb.stats, 2 * sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMallocHost((void **)&sl.h_stats, 2 * sizeof(unsigned long long)) != cudaSuccess)
     return fail(NGIA_E_NOMEM, "serve: slot allocation failed");
   sl.rb.cap = cap;
   for (int k = 0; k < kServeClasses; k++) {
@@ -800,6 +856,8 @@ extern "C" int ngia_serve_poll(ngia_server *s, int64_t ticket, int32_t wait_ms, 
   res->done = 1;
   res->resident = rq->resident;
   res->new_reps = rq->new_reps;
+  res->pairs = rq->pairs;
+  res->cells = rq->cells;
   s->requests.erase(it);
   return NGIA_OK;
 }

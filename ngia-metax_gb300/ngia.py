@@ -54,7 +54,7 @@ class ServeConfig(C.Structure):
 class ServeResult(C.Structure):
     _fields_ = [("done", C.c_int32), ("slot", C.c_int32), ("rounds", C.c_int32), ("resident", C.c_int32),
                 ("new_reps", C.c_int32), ("reserved", C.c_int32), ("queued_ms", C.c_double),
-                ("run_ms", C.c_double)]
+                ("run_ms", C.c_double), ("pairs", C.c_int64), ("cells", C.c_int64)]
 
 
 class Stats(C.Structure):

@@ -137,6 +137,17 @@ def test_word_orders_agree(cuda_device, order, monkeypatch):
         _check_cluster(db, ngia.params_clamp(0, s, 5, 0), modes=(ngia.MODE_GRAPH,))
 
 
+@pytest.mark.parametrize("warp_pairs", ["0", "100000000"])
+@pytest.mark.parametrize("db_type,s,w", [(0, 0.85, 5), (0, 0.5, 4), (1, 0.9, 3)])
+def test_thread_and_warp_per_pair_agree(cuda_device, monkeypatch, warp_pairs, db_type, s, w):
+    """Every class forced to thread-per-pair (0) or warp-per-pair (always):
+    both give the oracle's clustering, long records (multi-strip bands)
+    included."""
+    monkeypatch.setenv("NGIA_WARP_PAIRS", warp_pairs)
+    db = noisy_db(db_type, 300, seed=44 + db_type, long_records=3)
+    _check_cluster(db, ngia.params_clamp(db_type, s, w, 0))
+
+
 def test_stepwise_equals_full(cuda_device):
     db = family_db(0, n=400, anc=8, seed=51)
     p = ngia.params_clamp(0, 0.85, 5, 0)
