@@ -563,24 +563,32 @@ __global__ void __launch_bounds__(kAlignThreads)
       for (int sidx = 0; sidx < strips; sidx++) {
         const int j = js + 32 * sidx + lane;
         const bool have = j <= je;
-        uint32_t row = have ? rows[j] : 0u, pl[P];
+        // a lane above the band holds 0: it neither generates nor propagates
+        // (and there is no row above it that could take its carry)
+        uint32_t row = have ? rows[j] : 0u, pl[P], rv[P];
 #pragma unroll
-        for (int p = 0; p < P; p++) pl[p] = have ? s_pl[j * P + p] : 0u;
+        for (int p = 0; p < P; p++) {
+          pl[p] = have ? s_pl[j * P + p] : 0u;
+          rv[p] = __brev(cur[p]);  // residue k's bit moves to the sign bit
+        }
         const uint32_t row0 = row;
         uint32_t cout = 0;
         for (int k = 0; k < cols; k++) {
           uint32_t x = row;
 #pragma unroll
-          for (int p = 0; p < P; p++) x &= ~(pl[p] ^ (0u - ((cur[p] >> k) & 1u)));
+          for (int p = 0; p < P; p++) {
+            x &= ~(pl[p] ^ (uint32_t)((int)rv[p] >> 31));
+            rv[p] <<= 1;
+          }
           uint32_t sum, gen;
           asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(sum), "=r"(gen) : "r"(row), "r"(x));
-          const uint32_t G = __ballot_sync(kFullMask, have && gen);
-          const uint32_t Pm = __ballot_sync(kFullMask, have && sum == 0xFFFFFFFFu);
+          const uint32_t G = __ballot_sync(kFullMask, gen);
+          const uint32_t Pm = __ballot_sync(kFullMask, sum == 0xFFFFFFFFu);
           const uint32_t X = G | Pm;
           const unsigned long long tot = (unsigned long long)X + G + ((cmask >> k) & 1u);
           cout |= (uint32_t)(tot >> 32) << k;
           const uint32_t c = (((uint32_t)tot ^ X ^ G) >> lane) & 1u;
-          if (have) row = (sum + c) | (row ^ x);
+          row = (sum + c) | (row ^ x);  // stored only for lanes with a row
         }
         if (have) {
           rows[j] = row;
