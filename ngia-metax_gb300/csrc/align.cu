@@ -506,6 +506,133 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 // pair, all-ones until they enter the band), loaded at a strip's start and
 // stored at its end; after every query block the zero count (kept as the
 // sum of the lanes' row changes) gives the exact early rejection test.
+// sum = a + b over W words (word 0 lowest); returns the carry out.
+template <int W>
+__device__ __forceinline__ uint32_t add_words(const uint32_t (&a)[W], const uint32_t (&b)[W], uint32_t (&sum)[W]) {
+  uint32_t c;
+  if constexpr (W == 1) {
+    asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(sum[0]), "=r"(c) : "r"(a[0]), "r"(b[0]));
+  } else if constexpr (W == 2) {
+    asm("add.cc.u32 %0, %3, %5;\n\taddc.cc.u32 %1, %4, %6;\n\taddc.u32 %2, 0, 0;"
+        : "=r"(sum[0]), "=r"(sum[1]), "=r"(c)
+        : "r"(a[0]), "r"(a[1]), "r"(b[0]), "r"(b[1]));
+  } else {
+    static_assert(W == 4, "W is 1, 2 or 4");
+    asm("add.cc.u32 %0, %5, %9;\n\taddc.cc.u32 %1, %6, %10;\n\taddc.cc.u32 %2, %7, %11;\n\t"
+        "addc.cc.u32 %3, %8, %12;\n\taddc.u32 %4, 0, 0;"
+        : "=r"(sum[0]), "=r"(sum[1]), "=r"(sum[2]), "=r"(sum[3]), "=r"(c)
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]));
+  }
+  return c;
+}
+
+// sum += c (0 or 1) over W words; the carry out is dropped.
+template <int W>
+__device__ __forceinline__ void carry_in_words(uint32_t (&sum)[W], uint32_t c) {
+  if constexpr (W == 1) {
+    sum[0] += c;
+  } else if constexpr (W == 2) {
+    asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, 0;" : "+r"(sum[0]), "+r"(sum[1]) : "r"(c));
+  } else {
+    asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, 0;\n\taddc.cc.u32 %2, %2, 0;\n\taddc.u32 %3, %3, 0;"
+        : "+r"(sum[0]), "+r"(sum[1]), "+r"(sum[2]), "+r"(sum[3])
+        : "r"(c));
+  }
+}
+
+// Banded LCS of one pair by one warp, W row words per lane; returns the
+// zero count, or -1 when may_reject and the pair cannot reach the cutoff.
+template <int P, int W>
+__device__ __forceinline__ int warp_pair(uint32_t *rows, const uint32_t *s_pl, int nb1, uint32_t vlast,
+                                         const uint32_t *qpl, int nq, int lastcols, int B, int net2, int cutoff,
+                                         bool may_reject, int lane, unsigned long long &n_done) {
+  for (int j = lane; j < nb1; j += 32) rows[j] = 0xFFFFFFFFu;
+  __syncwarp();
+  int delta = 0;
+  uint32_t nxt[P];
+#pragma unroll
+  for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + p);
+  for (int i = 0; i < nq; i++) {
+    uint32_t cur[P];
+#pragma unroll
+    for (int p = 0; p < P; p++) {
+      cur[p] = nxt[p];
+      if (i + 1 < nq) nxt[p] = __ldg(qpl + (i + 1) * P + p);
+    }
+    const int js = max(i - B, 0), je = min(i + B, nb1 - 1);
+    const int strips = je >= js ? (je - js + 32 * W) / (32 * W) : 0;
+    const int cols = (i == nq - 1) ? lastcols : 32;
+    if (lane == 0) n_done += (unsigned long long)(je - js + 1) * cols;
+    uint32_t cmask = 0;  // carry into the strip, bit k for column k
+    for (int sidx = 0; sidx < strips; sidx++) {
+      // lane l holds the W consecutive rows j0 .. j0+W-1 of the strip; rows
+      // above the band hold 0: they neither generate nor propagate (and no
+      // row above them could take their carry)
+      const int j0 = js + 32 * W * sidx + W * lane;
+      uint32_t row[W], row0[W], pl[W][P], rv[P];
+#pragma unroll
+      for (int w = 0; w < W; w++) {
+        const bool have = j0 + w <= je;
+        row[w] = have ? rows[j0 + w] : 0u;
+        row0[w] = row[w];
+#pragma unroll
+        for (int p = 0; p < P; p++) pl[w][p] = have ? s_pl[(j0 + w) * P + p] : 0u;
+      }
+#pragma unroll
+      for (int p = 0; p < P; p++) rv[p] = __brev(cur[p]);  // residue k's bit moves to the sign bit
+      uint32_t cout = 0;
+      for (int k = 0; k < cols; k++) {
+        uint32_t m[P], x[W], sum[W];
+#pragma unroll
+        for (int p = 0; p < P; p++) {
+          m[p] = (uint32_t)((int)rv[p] >> 31);
+          rv[p] <<= 1;
+        }
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+          x[w] = row[w];
+#pragma unroll
+          for (int p = 0; p < P; p++) x[w] &= ~(pl[w][p] ^ m[p]);
+        }
+        const uint32_t gen = add_words<W>(row, x, sum);
+        uint32_t ones = sum[0];
+#pragma unroll
+        for (int w = 1; w < W; w++) ones &= sum[w];
+        const uint32_t G = __ballot_sync(kFullMask, gen);
+        const uint32_t Pm = __ballot_sync(kFullMask, ones == 0xFFFFFFFFu);
+        const uint32_t X = G | Pm;
+        const unsigned long long tot = (unsigned long long)X + G + ((cmask >> k) & 1u);
+        cout |= (uint32_t)(tot >> 32) << k;
+        carry_in_words<W>(sum, (((uint32_t)tot ^ X ^ G) >> lane) & 1u);
+#pragma unroll
+        for (int w = 0; w < W; w++) row[w] = sum[w] | (row[w] ^ x[w]);  // stored only for rows in the band
+      }
+#pragma unroll
+      for (int w = 0; w < W; w++) {
+        const int j = j0 + w;
+        if (j > je) continue;
+        rows[j] = row[w];
+        const uint32_t mk = (j == nb1 - 1) ? vlast : 0xFFFFFFFFu;
+        delta += __popc(~row[w] & mk) - __popc(~row0[w] & mk);
+      }
+      cmask = cout;
+    }
+    __syncwarp();  // this block's rows are stored before the next block loads them
+    if (may_reject && i + 1 < nq) {
+      int z = delta;
+#pragma unroll
+      for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(kFullMask, z, o);
+      if (z + (net2 - 32 * (i + 1)) < cutoff) {  // cannot reach the cutoff any more
+        return -1;
+      }
+    }
+  }
+  int sum = delta;
+#pragma unroll
+  for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFullMask, sum, o);
+  return sum;
+}
+
 template <int P>
 __global__ void __launch_bounds__(kAlignThreads)
     k_align_warp(DevDB db, RunBufs rb, RunParams prm, int cls, int score_mode, int warp_pairs) {
@@ -541,77 +668,16 @@ __global__ void __launch_bounds__(kAlignThreads)
       if (lane == 0) finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, 0, cutoff, L2, net2, qpl, s_list, n_members);
       continue;
     }
-    for (int j = lane; j < nb1; j += 32) rows[j] = 0xFFFFFFFFu;
-    __syncwarp();
-    int delta = 0;
-    bool rejected = false;
-    uint32_t nxt[P];
-#pragma unroll
-    for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + p);
-    for (int i = 0; i < nq; i++) {
-      uint32_t cur[P];
-#pragma unroll
-      for (int p = 0; p < P; p++) {
-        cur[p] = nxt[p];
-        if (i + 1 < nq) nxt[p] = __ldg(qpl + (i + 1) * P + p);
-      }
-      const int js = max(i - B, 0), je = min(i + B, nb1 - 1);
-      const int strips = je >= js ? (je - js + 32) >> 5 : 0;
-      const int cols = (i == nq - 1) ? lastcols : 32;
-      if (!score_mode && lane == 0) n_done += (unsigned long long)(je - js + 1) * cols;
-      uint32_t cmask = 0;  // carry into the strip, bit k for column k
-      for (int sidx = 0; sidx < strips; sidx++) {
-        const int j = js + 32 * sidx + lane;
-        const bool have = j <= je;
-        // a lane above the band holds 0: it neither generates nor propagates
-        // (and there is no row above it that could take its carry)
-        uint32_t row = have ? rows[j] : 0u, pl[P], rv[P];
-#pragma unroll
-        for (int p = 0; p < P; p++) {
-          pl[p] = have ? s_pl[j * P + p] : 0u;
-          rv[p] = __brev(cur[p]);  // residue k's bit moves to the sign bit
-        }
-        const uint32_t row0 = row;
-        uint32_t cout = 0;
-        for (int k = 0; k < cols; k++) {
-          uint32_t x = row;
-#pragma unroll
-          for (int p = 0; p < P; p++) {
-            x &= ~(pl[p] ^ (uint32_t)((int)rv[p] >> 31));
-            rv[p] <<= 1;
-          }
-          uint32_t sum, gen;
-          asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(sum), "=r"(gen) : "r"(row), "r"(x));
-          const uint32_t G = __ballot_sync(kFullMask, gen);
-          const uint32_t Pm = __ballot_sync(kFullMask, sum == 0xFFFFFFFFu);
-          const uint32_t X = G | Pm;
-          const unsigned long long tot = (unsigned long long)X + G + ((cmask >> k) & 1u);
-          cout |= (uint32_t)(tot >> 32) << k;
-          const uint32_t c = (((uint32_t)tot ^ X ^ G) >> lane) & 1u;
-          row = (sum + c) | (row ^ x);  // stored only for lanes with a row
-        }
-        if (have) {
-          rows[j] = row;
-          const uint32_t m = (j == nb1 - 1) ? vlast : 0xFFFFFFFFu;
-          delta += __popc(~row & m) - __popc(~row0 & m);
-        }
-        cmask = cout;
-      }
-      __syncwarp();  // this block's rows are stored before the next block loads them
-      if (!score_mode && i + 1 < nq) {
-        int z = delta;
-#pragma unroll
-        for (int o = 16; o; o >>= 1) z += __shfl_xor_sync(kFullMask, z, o);
-        if (z + (net2 - 32 * (i + 1)) < cutoff) {  // cannot reach the cutoff any more
-          rejected = true;
-          break;
-        }
-      }
-    }
-    if (rejected) continue;
-    int sum = delta;
-#pragma unroll
-    for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFullMask, sum, o);
+    // row words per lane by this pair's band window: 32 rows per strip up to
+    // windows of 32 blocks, then 64, then 128
+    const int A = window_of(B, nb1);
+    const int sum = A <= 32   ? warp_pair<P, 1>(rows, s_pl, nb1, vlast, qpl, nq, lastcols, B, net2, cutoff, !score_mode,
+                                                lane, n_done)
+                    : A <= 64 ? warp_pair<P, 2>(rows, s_pl, nb1, vlast, qpl, nq, lastcols, B, net2, cutoff, !score_mode,
+                                                lane, n_done)
+                              : warp_pair<P, 4>(rows, s_pl, nb1, vlast, qpl, nq, lastcols, B, net2, cutoff, !score_mode,
+                                                lane, n_done);
+    if (sum < 0) continue;  // rejected early
     if (lane == 0) finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, sum, cutoff, L2, net2, qpl, s_list, n_members);
     __syncwarp();
   }
@@ -621,8 +687,10 @@ __global__ void __launch_bounds__(kAlignThreads)
 // ---- dispatch ---------------------------------------------------------------------
 typedef void (*AlignFn)(DevDB, RunBufs, RunParams, int, int, int);
 
-static AlignFn warp_fn(int type) { return type == 0 ? k_align_warp<2> : k_align_warp<5>; }
-constexpr int kWarpKernel = kNumClasses;  // index of the warp kernel in the attribute table
+static AlignFn warp_fn(int type, int cls) {
+  (void)cls;
+  return type == 0 ? k_align_warp<2> : k_align_warp<5>;
+}constexpr int kWarpKernel = kNumClasses;  // index of the warp kernel in the attribute table
 
 static AlignFn align_fn(int type, int cls) {
   if (type == 0) {
@@ -672,9 +740,15 @@ cudaError_t align_configure(int type, int max_nb) {
     const int want = (int)align_smem(type, max_nb, c);
     int &have = configured[dev][type ? 1 : 0][c];
     if (want <= have) continue;
-    const void *fn = c == kWarpKernel ? (const void *)warp_fn(type) : (const void *)align_fn(type, c);
-    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, want);
-    if (e != cudaSuccess) return e;
+    if (c == kWarpKernel) {
+      for (int k = 0; k < num_classes(type); k++) {
+        e = cudaFuncSetAttribute((const void *)warp_fn(type, k), cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+        if (e != cudaSuccess) return e;
+      }
+    } else {
+      e = cudaFuncSetAttribute((const void *)align_fn(type, c), cudaFuncAttributeMaxDynamicSharedMemorySize, want);
+      if (e != cudaSuccess) return e;
+    }
     have = want;
   }
   return cudaSuccess;
@@ -684,7 +758,7 @@ cudaError_t align_configure(int type, int max_nb) {
 // (cls = kNumClasses: the warp kernel.)
 int align_occupancy(int type, int cls, int max_nb) {
   int nb = 0;
-  const void *fn = cls == kWarpKernel ? (const void *)warp_fn(type) : (const void *)align_fn(type, cls);
+  const void *fn = cls == kWarpKernel ? (const void *)warp_fn(type, num_classes(type) - 1) : (const void *)align_fn(type, cls);
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, kAlignThreads, align_smem(type, max_nb, cls)) !=
       cudaSuccess)
     return 1;
@@ -706,7 +780,7 @@ cudaError_t launch_align(ngia_ctx *c, int cls, cudaStream_t s, int score_mode) {
   cudaError_t e = cudaLaunchKernel((const void *)fn, dim3(c->grid_align[cls]), dim3(kAlignThreads), args,
                                    align_smem(c->db.type, c->db.max_nb, cls), s);
   if (e != cudaSuccess || wp < 0) return e;
-  return cudaLaunchKernel((const void *)warp_fn(c->db.type), dim3(c->grid_warp), dim3(kAlignThreads), args,
+  return cudaLaunchKernel((const void *)warp_fn(c->db.type, cls), dim3(c->grid_warp), dim3(kAlignThreads), args,
                           align_smem(c->db.type, c->db.max_nb, kWarpKernel), s);
 }
 
