@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--batch-max-seqs", type=int, default=200000)
     ap.add_argument("--serve-batches", type=int, default=200)
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrivals, batches per second")
-    ap.add_argument("--serve-slots", type=int, default=8)
+    ap.add_argument("--serve-slots", type=int, default=16)
     ap.add_argument("--n-seqs", type=int, default=0, help="override the sequence count (testing only)")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--mode", default="graph", choices=["graph", "plain"])

@@ -58,13 +58,21 @@ struct AlignHdr {
 // when the short-word test follows the alignment, its k-mer bitset) into
 // shared memory with bulk copies.  Returns false when there is no work.
 template <int P>
+// warp_mode: 1 for the warp-per-pair kernel (works on classes with at most
+// warp_pairs pairs), 0 for the thread-per-pair kernels (more than that); the
+// other kernel of a class returns here, before any staging.
 __device__ __forceinline__ bool align_setup(const DevDB &db, const RunBufs &rb, const RunParams &prm, int cls,
-                                            int score_mode, uint32_t *smem, uint64_t *bar, AlignHdr &h) {
+                                            int score_mode, int warp_pairs, int warp_mode, uint32_t *smem,
+                                            uint64_t *bar, AlignHdr &h) {
   __shared__ int s_hdr[6];
   RunState *st = rb.st;
   if (threadIdx.x == 0) {
     const bool skip = !score_mode && (st->done || st->iter >= st->iter_limit || st->err);
-    s_hdr[0] = skip ? 0 : (int)st->qcount[cls];
+    const int qn = skip ? 0 : (int)st->qcount[cls];
+    const bool mine = warp_mode ? qn <= warp_pairs : qn > warp_pairs;
+    // warp-per-pair: one pair per warp of this CTA
+    const bool idle = warp_mode && (int)(blockIdx.x * (blockDim.x >> 5)) >= qn;
+    s_hdr[0] = mine && !idle ? qn : 0;
     s_hdr[1] = st->rep_len;
     s_hdr[2] = st->rep_net;
     s_hdr[3] = st->rep_nb;
@@ -182,8 +190,7 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
   AlignHdr h;
-  if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
-  if (h.qn <= warp_pairs) return;  // few pairs: k_align_warp takes them
+  if (!align_setup<P>(db, rb, prm, cls, score_mode, warp_pairs, 0, smem, &bar, h)) return;
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
   RunState *st = rb.st;
@@ -350,8 +357,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
   AlignHdr h;
-  if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
-  if (h.qn <= warp_pairs) return;  // few pairs: k_align_warp takes them
+  if (!align_setup<P>(db, rb, prm, cls, score_mode, warp_pairs, 0, smem, &bar, h)) return;
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
   RunState *st = rb.st;
@@ -639,8 +645,7 @@ __global__ void __launch_bounds__(kAlignThreads)
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
   AlignHdr h;
-  if (!align_setup<P>(db, rb, prm, cls, score_mode, smem, &bar, h)) return;
-  if (h.qn > warp_pairs) return;  // many pairs: the thread-per-pair kernel takes them
+  if (!align_setup<P>(db, rb, prm, cls, score_mode, warp_pairs, 1, smem, &bar, h)) return;
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

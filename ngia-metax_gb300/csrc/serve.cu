@@ -383,11 +383,15 @@ bool trace() {
   return on;
 }
 
-// Driver of the leftover clustering: NGIA_SERVE_LEFTOVERS=plain|graph.
+// Driver of the leftover clustering (NGIA_SERVE_LEFTOVERS=plain|graph).  The
+// plain host loop is the default: a slot's database changes with every batch,
+// so the graph form would be captured and instantiated per batch, and with
+// several slots doing that at once it served 2.2x fewer queries per second
+// on GB300 (200 batches of the serving workload, 8 slots).
 int leftover_mode() {
   static const int m = [] {
     const char *t = getenv("NGIA_SERVE_LEFTOVERS");
-    return t && std::strcmp(t, "plain") == 0 ? NGIA_MODE_PLAIN : NGIA_MODE_GRAPH;
+    return t && std::strcmp(t, "graph") == 0 ? NGIA_MODE_GRAPH : NGIA_MODE_PLAIN;
   }();
   return m;
 }
