@@ -326,6 +326,15 @@ int ngia_rep_scores_noalloc(const uint32_t *d_words, int64_t rep_off,
                             const int64_t *d_query_off, int32_t n, int32_t type,
                             float similarity, int32_t *d_scores, void *stream);
 
+/* Loads another database into an open context, reusing its device memory
+ * (one host-to-device copy of the records and offsets, then the header
+ * arrays are rebuilt on the device).  The database must fit what the context
+ * was opened with: at most as many records and words, records of at most as
+ * many plane blocks (NGIA_E_LIMIT otherwise); same sequence type.  A run in
+ * progress ends; a captured graph is kept when the new database has the same
+ * record count, longest record and short-record flag. */
+int ngia_reload(ngia_ctx *ctx, const ngia_db_view *db);
+
 /* CUDA stream the context launches on (as an opaque handle, for timing). */
 void *ngia_stream(ngia_ctx *ctx);
 

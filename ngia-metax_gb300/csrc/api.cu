@@ -363,14 +363,39 @@ int ngia::drv::reload_ctx(ngia_ctx *c, const ngia_db_view *v) {
   if (v->n > c->cap_n || v->n_words > c->cap_words)
     return fail(NGIA_E_LIMIT, "reload: %d records / %lld words exceed the capacity (%lld / %lld)", v->n,
                 (long long)v->n_words, (long long)c->cap_n, (long long)c->cap_words);
-  destroy_graph(c);  // kernel arguments captured in a graph hold the old sizes
+  // longest record, checked on the host before anything is copied
+  int nb = 0;
+  for (int32_t i = 0; i < v->n; i++) {
+    const int64_t o = v->rec_off[i];
+    if (o < 0 || o + 2 > v->n_words) return fail(NGIA_E_FORMAT, "reload: record %d offset out of range", i);
+    nb = std::max(nb, (int)((v->words[o + 1] + 31) / 32));
+  }
+  if (nb > c->cap_nb)
+    return fail(NGIA_E_LIMIT, "reload: a record of %d blocks exceeds the capacity of %d", nb, c->cap_nb);
+  const ngia::DevDB before = c->db;
+  const int grids_before = c->grid_filter, warp_before = c->grid_warp;
   c->begun = false;
   int rc = load_db(c, v);
-  if (rc) return rc;
-  if (c->db.max_nb > c->cap_nb)
+  if (rc) {
+    destroy_graph(c);
+    return rc;
+  }
+  if (c->db.max_nb > c->cap_nb) {
+    destroy_graph(c);
     return fail(NGIA_E_LIMIT, "reload: a record of %d blocks exceeds the capacity of %d", c->db.max_nb, c->cap_nb);
-  size_grids(c, true);
+  }
+  size_grids(c, c->batch_member);
+  // a captured graph holds the kernel arguments (sizes) and grids: it stays
+  // valid when the database has the same shape
+  const bool same = before.n == c->db.n && before.max_nb == c->db.max_nb && before.has_short == c->db.has_short &&
+                    grids_before == c->grid_filter && warp_before == c->grid_warp;
+  if (!same) destroy_graph(c);
   return NGIA_OK;
+}
+
+extern "C" int ngia_reload(ngia_ctx *c, const ngia_db_view *v) {
+  ngia::clear_error();
+  return ngia::drv::reload_ctx(c, v);
 }
 
 extern "C" int ngia_close(ngia_ctx *c) {

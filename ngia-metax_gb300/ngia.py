@@ -120,6 +120,7 @@ def lib() -> C.CDLL:
         "ngia_serve_poll": (C.c_int, [VP, I64, I32, P(I32), P(I32), P(ServeResult)]),
         "ngia_serve_close": (C.c_int, [VP]),
         "ngia_close": (C.c_int, [VP]),
+        "ngia_reload": (C.c_int, [VP, P(DBView)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -450,6 +451,11 @@ class Context:
         st = Stats()
         _check(lib().ngia_cluster(self._h, C.byref(params), mode, _i32p(cl), _i32p(ident), C.byref(st)))
         return cl, ident, st.as_dict()
+
+    def reload(self, db) -> None:
+        """Loads another database (within this context's capacity) in place."""
+        _check(lib().ngia_reload(self._h, C.byref(db.view)))
+        self.db = db
 
     def begin(self, params: Params, mode: int = MODE_GRAPH) -> None:
         _check(lib().ngia_cluster_begin(self._h, C.byref(params), mode))

@@ -148,6 +148,28 @@ def test_thread_and_warp_per_pair_agree(cuda_device, monkeypatch, warp_pairs, db
     _check_cluster(db, ngia.params_clamp(db_type, s, w, 0))
 
 
+def test_reload_reuses_the_context(cuda_device):
+    """ngia_reload: the same database again (graph kept), a smaller one, and
+    one that does not fit."""
+    big = family_db(0, n=400, anc=8, seed=52)
+    small = family_db(0, n=150, anc=4, seed=53, len_max=600)
+    p = ngia.params_clamp(0, 0.85, 5, 0)
+    exp_big = oracle.cluster(big.words, big.rec_off, 0, p.similarity, p.word_length, p.precise)
+    exp_small = oracle.cluster(small.words, small.rec_off, 0, p.similarity, p.word_length, p.precise)
+    with ngia.Context(big) as ctx:
+        first = ctx.cluster(p, ngia.MODE_GRAPH)
+        ctx.reload(big)
+        again = ctx.cluster(p, ngia.MODE_GRAPH)
+        ctx.reload(small)
+        sm = ctx.cluster(p, ngia.MODE_GRAPH)
+        sm_plain = ctx.cluster(p, ngia.MODE_PLAIN)
+        with pytest.raises(ngia.NgiaError) as ex:
+            ctx.reload(family_db(0, n=500, anc=8, seed=54))
+        assert ex.value.code == -8
+    for got, exp in ((first, exp_big), (again, exp_big), (sm, exp_small), (sm_plain, exp_small)):
+        assert np.array_equal(got[0], exp[0]) and np.array_equal(got[1], exp[1])
+
+
 def test_stepwise_equals_full(cuda_device):
     db = family_db(0, n=400, anc=8, seed=51)
     p = ngia.params_clamp(0, 0.85, 5, 0)
