@@ -326,6 +326,16 @@ int ngia_rep_scores_noalloc(const uint32_t *d_words, int64_t rep_off,
                             const int64_t *d_query_off, int32_t n, int32_t type,
                             float similarity, int32_t *d_scores, void *stream);
 
+/* Checkpoint of a run in progress (after ngia_cluster_begin / _step): the
+ * run state, the unclustered set, the assignment and scores, and the
+ * parameters, written to `path` (via a temporary file, then renamed).  No
+ * counterpart in the reference.  ngia_cluster_resume continues such a run in
+ * a context holding the same database (checked by record count, word count
+ * and a hash of the records; NGIA_E_FORMAT for another database or a damaged
+ * file), with either driver; the run then ends exactly as if uninterrupted. */
+int ngia_cluster_save(ngia_ctx *ctx, const char *path);
+int ngia_cluster_resume(ngia_ctx *ctx, const char *path, int32_t mode);
+
 /* Loads another database into an open context, reusing its device memory
  * (one host-to-device copy of the records and offsets, then the header
  * arrays are rebuilt on the device).  The database must fit what the context

@@ -64,6 +64,9 @@ int reload_ctx(ngia_ctx *c, const ngia_db_view *v);
 // begin a run whose unclustered set is the given device bitmap (bit i =
 // sequence i takes part), instead of every sequence.
 int begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, const uint32_t *d_alive);
+// graph form of the greedy loop (captured once per parameter set)
+int build_graph(ngia_ctx *c);
+void destroy_graph(ngia_ctx *c);
 int pull_state(ngia_ctx *c);
 int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond);
 void fill_stats(const ngia_ctx *c, ngia_stats *stats);

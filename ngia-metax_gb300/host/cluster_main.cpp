@@ -5,6 +5,7 @@
 // and writes <outdir>/cluster.txt and <outdir>/represent.fasta.
 // Environment: NGIA_MODE=plain|graph (default graph) selects the driver form;
 // NGIA_IDENTITY=<path> also writes "index<TAB>representative<TAB>score" lines.
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -75,8 +76,32 @@ int main(int argc, char **argv) {
   rc = ngia_open(&db->view, &ctx);
   if (rc) die("ngia_open", rc);
   std::vector<int32_t> cluster((size_t)db->view.n), ident((size_t)db->view.n);
-  rc = ngia_cluster(ctx, &p, mode, cluster.data(), ident.data(), nullptr);
-  if (rc) die("ngia_cluster", rc);
+  // NGIA_CHECKPOINT=<file>: resume from the file when it exists and save the
+  // run to it every NGIA_CHECKPOINT_EVERY representatives (default 10,000)
+  const char *ck = std::getenv("NGIA_CHECKPOINT");
+  if (!ck || !*ck) {
+    rc = ngia_cluster(ctx, &p, mode, cluster.data(), ident.data(), nullptr);
+    if (rc) die("ngia_cluster", rc);
+  } else {
+    int64_t every = 10000;
+    if (const char *e = std::getenv("NGIA_CHECKPOINT_EVERY")) every = std::max<int64_t>(1, std::atoll(e));
+    FILE *probe = std::fopen(ck, "rb");
+    if (probe) {
+      std::fclose(probe);
+      rc = ngia_cluster_resume(ctx, ck, mode);
+      if (rc) die("resuming the checkpoint", rc);
+    } else {
+      rc = ngia_cluster_begin(ctx, &p, mode);
+      if (rc) die("ngia_cluster_begin", rc);
+    }
+    for (int32_t done = 0; !done;) {
+      rc = ngia_cluster_step(ctx, every, &done);
+      if (rc) die("ngia_cluster_step", rc);
+      if (!done && (rc = ngia_cluster_save(ctx, ck))) die("saving the checkpoint", rc);
+    }
+    rc = ngia_cluster_end(ctx, cluster.data(), ident.data(), nullptr);
+    if (rc) die("ngia_cluster_end", rc);
+  }
   ngia_close(ctx);
   std::cout << "\r" << db->view.n << "/" << db->view.n << "\n" << std::endl;
 

@@ -121,6 +121,8 @@ def lib() -> C.CDLL:
         "ngia_serve_close": (C.c_int, [VP]),
         "ngia_close": (C.c_int, [VP]),
         "ngia_reload": (C.c_int, [VP, P(DBView)]),
+        "ngia_cluster_save": (C.c_int, [VP, C.c_char_p]),
+        "ngia_cluster_resume": (C.c_int, [VP, C.c_char_p, I32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -456,6 +458,14 @@ class Context:
         """Loads another database (within this context's capacity) in place."""
         _check(lib().ngia_reload(self._h, C.byref(db.view)))
         self.db = db
+
+    def save(self, path: str) -> None:
+        """Checkpoint of the run in progress."""
+        _check(lib().ngia_cluster_save(self._h, str(path).encode()))
+
+    def resume(self, path: str, mode: int = MODE_GRAPH) -> None:
+        """Continues a checkpointed run of this context's database."""
+        _check(lib().ngia_cluster_resume(self._h, str(path).encode(), mode))
 
     def begin(self, params: Params, mode: int = MODE_GRAPH) -> None:
         _check(lib().ngia_cluster_begin(self._h, C.byref(params), mode))

@@ -170,6 +170,40 @@ def test_reload_reuses_the_context(cuda_device):
         assert np.array_equal(got[0], exp[0]) and np.array_equal(got[1], exp[1])
 
 
+@pytest.mark.parametrize("mode", [ngia.MODE_PLAIN, ngia.MODE_GRAPH])
+def test_checkpoint_resume(cuda_device, tmp_path, mode):
+    """A run saved after some iterations and resumed in another context ends
+    exactly as the uninterrupted run; foreign or damaged files are refused."""
+    db = family_db(0, n=400, anc=8, seed=55)
+    p = ngia.params_clamp(0, 0.85, 5, 0)
+    ck = tmp_path / "run.ckpt"
+    with ngia.Context(db) as ctx:
+        full = ctx.cluster(p, ngia.MODE_GRAPH)
+        ctx.begin(p, mode)
+        ctx.step(9)
+        ctx.save(ck)
+    with ngia.Context(db) as ctx:
+        ctx.resume(ck, mode)
+        while not ctx.step(50):
+            pass
+        cl, ident, st = ctx.end()
+    assert np.array_equal(cl, full[0]) and np.array_equal(ident, full[1])
+    assert st["iterations"] == full[2]["iterations"] and st["candidates"] == full[2]["candidates"]
+    other = family_db(0, n=400, anc=8, seed=56)
+    with ngia.Context(other) as ctx:
+        with pytest.raises(ngia.NgiaError) as ex:
+            ctx.resume(ck, mode)
+        assert ex.value.code == -3
+    raw = bytearray(ck.read_bytes())
+    raw[len(raw) // 2] ^= 0x40
+    bad = tmp_path / "bad.ckpt"
+    bad.write_bytes(bytes(raw))
+    with ngia.Context(db) as ctx:
+        with pytest.raises(ngia.NgiaError) as ex:
+            ctx.resume(bad, mode)
+        assert ex.value.code == -3
+
+
 def test_stepwise_equals_full(cuda_device):
     db = family_db(0, n=400, anc=8, seed=51)
     p = ngia.params_clamp(0, 0.85, 5, 0)
@@ -207,3 +241,30 @@ def test_cli_outputs_identical(cuda_device, tmp_path):
     for f in ("cluster.txt", "represent.fasta"):
         assert (o1 / f).read_bytes() == (o2 / f).read_bytes(), f
     assert "Cluster:\t" in r.stdout
+
+
+def test_cli_resumes_a_checkpoint(cuda_device, tmp_path):
+    """cluster with NGIA_CHECKPOINT: resumes a run saved through the C ABI and
+    writes the same files as an uninterrupted run."""
+    seq, off = ngia.synth(type=0, n_seqs=300, n_ancestors=6, len_a=500.0, len_b=50.0, len_min=300,
+                          len_max=700, seed=62)
+    fa = tmp_path / "in.fasta"
+    ngia.write_fasta(str(fa), seq, off, width=70)
+    dbdir, o1, o2 = tmp_path / "db", tmp_path / "plain", tmp_path / "resumed"
+    for d in (dbdir, o1, o2):
+        d.mkdir()
+    b = ROOT / "ngia-metax_gb300" / "_build"
+    subprocess.run([str(b / "makeDB"), "-i", str(fa), "-o", str(dbdir), "-t", "0"], check=True, capture_output=True)
+    args = ["-i", str(dbdir), "-w", "5", "-s", "0.85"]
+    subprocess.run([str(b / "cluster"), "-o", str(o1)] + args, check=True, capture_output=True)
+    db = ngia.DB.load(str(dbdir))
+    ck = tmp_path / "run.ckpt"
+    with ngia.Context(db) as ctx:
+        ctx.begin(ngia.params_clamp(0, 0.85, 5, 0), ngia.MODE_GRAPH)
+        ctx.step(11)
+        ctx.save(ck)
+    env = dict(os.environ, NGIA_CHECKPOINT=str(ck), NGIA_CHECKPOINT_EVERY="7")
+    r = subprocess.run([str(b / "cluster"), "-o", str(o2)] + args, capture_output=True, text=True, env=env)
+    assert r.returncode == 0, r.stderr
+    for f in ("cluster.txt", "represent.fasta"):
+        assert (o1 / f).read_bytes() == (o2 / f).read_bytes(), f
