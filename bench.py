@@ -287,7 +287,11 @@ def run_ours(args, dist: Dist):
                "wall_s_timed": t_wall,
                "roofline": {"bound": "int32", "kernel": "k_align_* (banded bit-parallel LCS)",
                             "achieved": done_gcell, "peak": peak_gcell, "unit": "Gcell/s",
-                            "frac": done_gcell / peak_gcell if peak_gcell else None, "traffic": None,
+                            "frac": done_gcell / peak_gcell if peak_gcell else None,
+                            "traffic": profiled_traffic(args),
+                            "traffic_note": "DRAM bytes per launch of k_align_tiled<2,64> from one ncu capture "
+                                            "(profiles/align_tiled_dna_1m.md); algorithmic: the query planes "
+                                            "of ~995k pairs, ~390 MB",
                             "peak_source": f"of measured INT32 issue rate {int_gops:.0f} Gop/s (probe) x 32 cells"
                                            f" / {ops} ops", "reference_cells_rate": band_gcell,
                             "profiled_iterations": prof_iters, "ms_align_per_iter": ms_align / prof_iters,
@@ -305,6 +309,21 @@ def run_ours(args, dist: Dist):
     db.close()
     if out is not None:
         print(json.dumps(out), flush=True)
+
+
+def profiled_traffic(args) -> int | None:
+    """DRAM bytes per launch of the dominant alignment kernel from the
+    committed ncu summary, when it was captured on this workload."""
+    path = ROOT / "profiles" / "align_tiled_dna_1m.md"
+    try:
+        text = path.read_text()
+    except OSError:
+        return None
+    fields = dict(line.split(": ", 1) for line in text.splitlines() if line.startswith("traffic_"))
+    want = f"{args.workload} s={args.similarity:g} w={args.word}"
+    if fields.get("traffic_workload") != want:
+        return None
+    return int(fields["traffic_bytes_per_launch"])
 
 
 def ngia_classes(db_type: int) -> int:
