@@ -784,7 +784,7 @@ cudaError_t launch_align(ngia_ctx *c, int cls, cudaStream_t s, int score_mode) {
   void *args[] = {&db, &rb, &prm, &cls, &score_mode, &wp};
   cudaError_t e = cudaLaunchKernel((const void *)fn, dim3(c->grid_align[cls]), dim3(kAlignThreads), args,
                                    align_smem(c->db.type, c->db.max_nb, cls), s);
-  if (e != cudaSuccess || wp < 0) return e;
+  if (e != cudaSuccess || wp <= 0) return e;  // no class can go warp-per-pair
   return cudaLaunchKernel((const void *)warp_fn(c->db.type, cls), dim3(c->grid_warp), dim3(kAlignThreads), args,
                           align_smem(c->db.type, c->db.max_nb, kWarpKernel), s);
 }

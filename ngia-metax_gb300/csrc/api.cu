@@ -145,6 +145,7 @@ int build_graph(ngia_ctx *c) {
     return fail(NGIA_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
   }
   c->graph_exec = exec;
+  c->graph_warp_pairs = c->warp_pairs;
   c->graph_ready = true;
   c->graph_prm = c->prm;
   return NGIA_OK;
@@ -260,13 +261,18 @@ void size_grids(ngia_ctx *c, bool by_size) {
   // that on a warp, at ~3x the instructions per cell)
   c->grid_warp = c->num_sms * ngia::align_occupancy(type, ngia::kNumClasses, c->cap_nb);
   c->warp_pairs = 2 * c->grid_warp * (ngia::align_threads() / 32);
-  if (const char *w = getenv("NGIA_WARP_PAIRS")) c->warp_pairs = atoi(w);
   if (by_size) {
     const int64_t n = std::max(1, c->db.n), nbw = (n + 31) / 32;
     const int by_n = (int)std::min<int64_t>((n + 127) / 128, INT32_MAX);
     for (int k = 0; k < ngia::num_classes(type); k++) c->grid_align[k] = std::max(1, std::min(c->grid_align[k], by_n));
     c->grid_filter = std::max(1, std::min(c->grid_filter, (int)((nbw + 7) / 8)));
+    // warp-per-pair: no more warps than the job has sequences
+    const int wpc = ngia::align_threads() / 32;
+    c->grid_warp = std::max(1, std::min(c->grid_warp, (int)((n + wpc - 1) / wpc)));
+    c->warp_pairs = 2 * c->grid_warp * wpc;
   }
+  if (const char *w = getenv("NGIA_WARP_PAIRS")) c->warp_pairs = atoi(w);
+  c->warp_pairs_default = c->warp_pairs;
 }
 
 // Run buffers for up to cap_n sequences whose records have up to cap_nb
@@ -474,7 +480,8 @@ int ngia::drv::begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, con
   if (d_alive) CK(ngia::launch_subset_start(c, d_alive));
   rc = pull_state(c);
   if (rc) return rc;
-  if (mode == NGIA_MODE_GRAPH && !(c->graph_ready && same_params(c->graph_prm, c->prm))) {
+  if (mode == NGIA_MODE_GRAPH &&
+      !(c->graph_ready && same_params(c->graph_prm, c->prm) && c->graph_warp_pairs == c->warp_pairs)) {
     rc = build_graph(c);
     if (rc) return rc;
   }

@@ -35,6 +35,8 @@ struct ngia_ctx {
   int grid_align[ngia::kNumClasses] = {0};
   int grid_warp = 0;    // CTAs of the warp-per-pair kernel
   int warp_pairs = -1;  // a class with at most this many pairs runs warp-per-pair
+  int warp_pairs_default = -1;  // the above as sized for this context's grids
+  int graph_warp_pairs = -1;    // warp_pairs the captured graph was built with
   // graph form of the greedy loop
   cudaGraphExec_t graph_exec = nullptr;
   cudaGraph_t graph = nullptr;
