@@ -64,6 +64,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--skip-drivers", action="store_true", help="skip the whole-job graph vs plain comparison")
     ap.add_argument("--cpu-only", action="store_true",
                     help="replica plumbing with the CPU oracle as the engine (tests; no GPU)")
     return ap.parse_args()
@@ -223,7 +224,9 @@ def run_ours(args, dist: Dist):
     p = ngia.params_clamp(cfg["type"], args.similarity, args.word, 0)
     mode = ngia.MODE_GRAPH if args.mode == "graph" else ngia.MODE_PLAIN
     S = args.iters_per_step
-    launches_per_iter = 3 + ngia_classes(cfg["type"])
+    # per iteration: prep, filter, next, and per class the thread-per-pair and
+    # the warp-per-pair kernel
+    launches_per_iter = 3 + 2 * ngia_classes(cfg["type"])
     int_gops = ngia.measure_int_peak() if dist.rank == 0 else 0.0
 
     ctx = ngia.Context(db)
@@ -265,6 +268,34 @@ def run_ours(args, dist: Dist):
     filt_gbs = (b["filter_bytes"] - a["filter_bytes"]) / (ms_filter * 1e-3) / 1e9
     ctx.close()
 
+    # whole jobs: the 20,000-sequence DNA configuration clustered to the end by
+    # the device-side graph driver and by the plain host loop
+    drivers = None
+    if dist.rank == 0 and not args.skip_drivers:
+        import numpy as np
+
+        small_cfg = dict(ngia.CONFIGS["dna_small"])
+        sq = ngia.synth(**small_cfg, seed=args.seed)
+        sdb = ngia.DB.pack(0, sq, sq.off)
+        sq.close()
+        sp = ngia.params_clamp(0, args.similarity, args.word, 0)
+        times, outs = {}, {}
+        with ngia.Context(sdb) as sctx:
+            for name, mode in (("graph", ngia.MODE_GRAPH), ("plain", ngia.MODE_PLAIN)):
+                sctx.cluster(sp, mode)  # warm-up (graph capture, caches)
+                t0 = time.perf_counter()
+                outs[name] = sctx.cluster(sp, mode)
+                times[name] = time.perf_counter() - t0
+        same = all(np.array_equal(a, b) for a, b in zip(outs["graph"][:2], outs["plain"][:2]))
+        drivers = {"workload": f"dna_small: {sdb.n:,} DNA sequences (400 ancestors) clustered to the end, "
+                               f"s={args.similarity}, w={args.word}",
+                   "representatives": int(outs["graph"][2]["iterations"]),
+                   "graph_s": times["graph"], "plain_s": times["plain"],
+                   "graph_seqs_per_s": sdb.n / times["graph"], "plain_seqs_per_s": sdb.n / times["plain"],
+                   "speedup": times["plain"] / times["graph"], "identical": bool(same),
+                   "timing": "host clock around ngia_cluster (assignment and scores returned)"}
+        sdb.close()
+
     out = None
     if dist.rank == 0:
         planes = 2 if cfg["type"] == 0 else 5
@@ -305,6 +336,7 @@ def run_ours(args, dist: Dist):
                                    "peak_source": peaks["source"],
                                    "ms_filter_per_iter": ms_filter / prof_iters},
                "gpu_launches": launches_per_iter * S * args.steps,
+               "drivers_whole_job": drivers,
                "clocks": clk, "cpu_baseline": cpu, "e2e": e2e}
     db.close()
     if out is not None:
