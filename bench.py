@@ -371,7 +371,7 @@ def run_e2e(args, db, p, S):
     ngia.pin_host(db.words)
     ngia.pin_host(db.rec_off)
     try:
-        times, cands = [], []
+        times, cands, dev = [], [], []
         with ngia.Context(db) as ctx:
             for k in range(1 + args.e2e_steps):
                 t0 = time.perf_counter()
@@ -383,12 +383,16 @@ def run_e2e(args, db, p, S):
                 if k:
                     times.append(dt)
                     cands.append(st["candidates"])
+                    dev.append(ctx.step_ms())
     finally:
         ngia.unpin_host(db.words)
         ngia.unpin_host(db.rec_off)
     T = sum(times)
     return {"value": sum(cands) / T, "unit": UNIT, "h2d_bytes_per_step": int(db.words.nbytes + db.rec_off.nbytes),
             "d2h_bytes_per_step": int(8 * db.n), "steps": len(times),
+            "device_ms_per_step": sum(dev) / len(dev), "wall_ms_per_step": 1e3 * T / len(times),
+            "iterations": f"greedy iterations 1-{S} of a fresh run every step (the most expensive ones: the "
+                          f"longest representatives)",
             "per_step": f"ngia_reload (database from pinned host memory into the open context) + {S} greedy "
                         f"iterations + ngia_cluster_end (assignment and scores to host); host clock"}
 

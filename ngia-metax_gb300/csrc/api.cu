@@ -257,10 +257,13 @@ void size_grids(ngia_ctx *c, bool by_size) {
     c->grid_align[k] = c->num_sms * ngia::align_occupancy(type, k, c->cap_nb);
   c->grid_filter = c->num_sms * 8;
   // warp-per-pair: the whole GPU's warps; a class goes warp-per-pair when it
-  // has at most two pairs per warp (the pair latency on one thread is ~20x
-  // that on a warp, at ~3x the instructions per cell)
+  // has at most one pair per warp (a wide pair's latency on a warp is a few
+  // times shorter than on a thread, at ~6x the instructions per cell; swept
+  // on GB300: 0.25, 0.5, 1 and 2 pairs per warp gave 41, 47, 47 and 40M
+  // candidate seqs/s on the 20,000-sequence DNA workload and within 1% of
+  // each other on the 1M DNA and 200k protein workloads)
   c->grid_warp = c->num_sms * ngia::align_occupancy(type, ngia::kNumClasses, c->cap_nb);
-  c->warp_pairs = 2 * c->grid_warp * (ngia::align_threads() / 32);
+  c->warp_pairs = c->grid_warp * (ngia::align_threads() / 32);
   if (by_size) {
     const int64_t n = std::max(1, c->db.n), nbw = (n + 31) / 32;
     const int by_n = (int)std::min<int64_t>((n + 127) / 128, INT32_MAX);
@@ -269,7 +272,7 @@ void size_grids(ngia_ctx *c, bool by_size) {
     // warp-per-pair: no more warps than the job has sequences
     const int wpc = ngia::align_threads() / 32;
     c->grid_warp = std::max(1, std::min(c->grid_warp, (int)((n + wpc - 1) / wpc)));
-    c->warp_pairs = 2 * c->grid_warp * wpc;
+    c->warp_pairs = c->grid_warp * wpc;
   }
   if (const char *w = getenv("NGIA_WARP_PAIRS")) c->warp_pairs = atoi(w);
   c->warp_pairs_default = c->warp_pairs;
