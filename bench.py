@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-drivers", action="store_true", help="skip the whole-job graph vs plain comparison")
+    ap.add_argument("--autotune", type=int, default=4, help="iterations per setting tried by ngia_autotune (0: off)")
     ap.add_argument("--cpu-only", action="store_true",
                     help="replica plumbing with the CPU oracle as the engine (tests; no GPU)")
     return ap.parse_args()
@@ -230,6 +231,7 @@ def run_ours(args, dist: Dist):
     int_gops = ngia.measure_int_peak() if dist.rank == 0 else 0.0
 
     ctx = ngia.Context(db)
+    tuning = ctx.autotune(p, args.autotune) if args.autotune > 0 else None  # before the timed region
     ctx.begin(p, mode)
     for _ in range(args.warmup):
         ctx.step(S)
@@ -337,6 +339,7 @@ def run_ours(args, dist: Dist):
                                    "ms_filter_per_iter": ms_filter / prof_iters},
                "gpu_launches": launches_per_iter * S * args.steps,
                "drivers_whole_job": drivers,
+               "tuning": tuning,
                "clocks": clk, "cpu_baseline": cpu, "e2e": e2e}
     db.close()
     if out is not None:

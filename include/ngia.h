@@ -336,6 +336,26 @@ int ngia_rep_scores_noalloc(const uint32_t *d_words, int64_t rep_off,
 int ngia_cluster_save(ngia_ctx *ctx, const char *path);
 int ngia_cluster_resume(ngia_ctx *ctx, const char *path, int32_t mode);
 
+/* Run-time tuning (no counterpart in the reference).  Three settings change
+ * the speed of a run, never its result: the order of the two cheap tests
+ * (short-word test before or after the alignment), the number of idle lanes
+ * a warp of the tiled alignment waits for before it claims new pairs, and
+ * the pair count up to which a class is aligned warp-per-pair.
+ * ngia_autotune times candidate settings on the first `iters` greedy
+ * iterations of a fresh run of this context's database (graph driver, device
+ * time), keeps the fastest for later runs of the context and reports it;
+ * ngia_set_tuning applies settings found before. */
+typedef struct ngia_tuning {
+    int32_t word_order;   /* 0 by similarity, 1 short words first, 2 alignment first */
+    int32_t refill;       /* 1..32 idle lanes                                        */
+    int32_t warp_pairs;   /* warp-per-pair up to this many pairs; -1 = default      */
+    int32_t candidates;   /* settings timed (ngia_autotune)                          */
+    double  ms_per_iter;  /* device time per iteration of the chosen setting         */
+    double  default_ms_per_iter;  /* the same for the default setting                */
+} ngia_tuning;
+int ngia_autotune(ngia_ctx *ctx, const ngia_params *p, int32_t iters, ngia_tuning *out);
+int ngia_set_tuning(ngia_ctx *ctx, const ngia_tuning *t);
+
 /* Loads another database into an open context, reusing its device memory
  * (one host-to-device copy of the records and offsets, then the header
  * arrays are rebuilt on the device).  The database must fit what the context

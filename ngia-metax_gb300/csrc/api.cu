@@ -470,10 +470,11 @@ int ngia::drv::begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, con
   c->prm.s = p->similarity;
   c->prm.w = p->word_length;
   c->prm.precise = p->precise;
-  c->prm.word_order = 0;
+  c->prm.word_order = c->tuned_word_order;
   if (const char *wo = getenv("NGIA_WORD_ORDER")) c->prm.word_order = atoi(wo);
-  c->prm.refill = 32;
+  c->prm.refill = c->tuned_refill;
   if (const char *rf = getenv("NGIA_REFILL")) c->prm.refill = std::max(1, std::min(32, atoi(rf)));
+  if (!getenv("NGIA_WARP_PAIRS")) c->warp_pairs = c->tuned_warp_pairs >= 0 ? c->tuned_warp_pairs : c->warp_pairs_default;
   if (c->db.has_short && !c->prm.precise) c->prm.word_order = 1;  // exact path is word first
   c->mode = mode;
   c->ms_filter = c->ms_align = 0.0;

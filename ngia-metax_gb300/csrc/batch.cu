@@ -61,7 +61,7 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
     // one job after the other, host loop per representative
     for (size_t j = 0; j < nj; j++) {
       ngia_ctx *c = b->jobs[j];
-      c->warp_pairs = c->warp_pairs_default;
+      c->tuned_warp_pairs = -1;
       int rc = ngia_cluster_begin(c, &params[j], NGIA_MODE_PLAIN);
       if (rc) return rc;
       int32_t done = 0;
@@ -76,7 +76,7 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
       // jobs running side by side fill the GPU: one thread per pair, the
       // form with the fewest instructions per cell (256-job batch on GB300:
       // 15.4M vs 13.0M candidate seqs/s with warp-per-pair classes)
-      c->warp_pairs = getenv("NGIA_WARP_PAIRS") ? c->warp_pairs_default : 0;
+      c->tuned_warp_pairs = 0;
       int rc = ngia_cluster_begin(c, &params[j], NGIA_MODE_GRAPH);
       if (rc) return rc;
       c->h_state->iter_limit = max_iters > 0 ? max_iters : INT64_MAX;

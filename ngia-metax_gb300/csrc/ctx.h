@@ -36,6 +36,10 @@ struct ngia_ctx {
   int grid_warp = 0;    // CTAs of the warp-per-pair kernel
   int warp_pairs = -1;  // a class with at most this many pairs runs warp-per-pair
   int warp_pairs_default = -1;  // the above as sized for this context's grids
+  // settings that change speed only (set by ngia_autotune / ngia_set_tuning):
+  // test order (0 auto, 1 short words first, 2 alignment first), lockstep
+  // refill threshold, warp-per-pair cut-off (-1: keep warp_pairs_default)
+  int tuned_word_order = 0, tuned_refill = 32, tuned_warp_pairs = -1;
   int graph_warp_pairs = -1;    // warp_pairs the captured graph was built with
   // graph form of the greedy loop
   cudaGraphExec_t graph_exec = nullptr;

@@ -57,6 +57,11 @@ class ServeResult(C.Structure):
                 ("run_ms", C.c_double), ("pairs", C.c_int64), ("cells", C.c_int64)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("word_order", C.c_int32), ("refill", C.c_int32), ("warp_pairs", C.c_int32),
+                ("candidates", C.c_int32), ("ms_per_iter", C.c_double), ("default_ms_per_iter", C.c_double)]
+
+
 class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("iterations", "candidates", "base_pass", "align_pairs", "members",
                                          "band_cells", "filter_bytes", "word_checks", "done_cells")] + \
@@ -122,6 +127,8 @@ def lib() -> C.CDLL:
         "ngia_close": (C.c_int, [VP]),
         "ngia_reload": (C.c_int, [VP, P(DBView)]),
         "ngia_cluster_save": (C.c_int, [VP, C.c_char_p]),
+        "ngia_autotune": (C.c_int, [VP, P(Params), I32, P(Tuning)]),
+        "ngia_set_tuning": (C.c_int, [VP, P(Tuning)]),
         "ngia_cluster_resume": (C.c_int, [VP, C.c_char_p, I32]),
     }
     for name, (res, args) in sig.items():
@@ -458,6 +465,16 @@ class Context:
         """Loads another database (within this context's capacity) in place."""
         _check(lib().ngia_reload(self._h, C.byref(db.view)))
         self.db = db
+
+    def autotune(self, params: Params, iters: int = 4) -> dict:
+        """Times the speed-only settings on the first iterations; keeps the fastest."""
+        t = Tuning()
+        _check(lib().ngia_autotune(self._h, C.byref(params), iters, C.byref(t)))
+        return {f: getattr(t, f) for f, _ in Tuning._fields_}
+
+    def set_tuning(self, word_order: int = 0, refill: int = 32, warp_pairs: int = -1) -> None:
+        t = Tuning(word_order, refill, warp_pairs, 0, 0.0, 0.0)
+        _check(lib().ngia_set_tuning(self._h, C.byref(t)))
 
     def save(self, path: str) -> None:
         """Checkpoint of the run in progress."""

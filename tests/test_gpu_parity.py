@@ -204,6 +204,26 @@ def test_checkpoint_resume(cuda_device, tmp_path, mode):
         assert ex.value.code == -3
 
 
+@pytest.mark.parametrize("db_type,s,w", [(0, 0.85, 5), (0, 0.95, 5), (1, 0.9, 3)])
+def test_tuning_changes_speed_not_results(cuda_device, db_type, s, w):
+    """ngia_autotune and explicit settings: the clustering stays the oracle's."""
+    db = noisy_db(db_type, 300, seed=66 + db_type, long_records=2)
+    p = ngia.params_clamp(db_type, s, w, 0)
+    ocl, oid, _ = oracle.cluster(db.words, db.rec_off, db_type, p.similarity, p.word_length, p.precise)
+    with ngia.Context(db) as ctx:
+        t = ctx.autotune(p, iters=3)
+        assert t["candidates"] >= 6 and t["ms_per_iter"] > 0
+        got = [ctx.cluster(p, ngia.MODE_GRAPH)]
+        for wo, rf, wp in ((1, 24, 0), (2, 1, 10 ** 8), (0, 32, -1)):
+            ctx.set_tuning(wo, rf, wp)
+            got.append(ctx.cluster(p, ngia.MODE_GRAPH))
+            got.append(ctx.cluster(p, ngia.MODE_PLAIN))
+        with pytest.raises(ngia.NgiaError):
+            ctx.set_tuning(3, 32, -1)
+    for cl, ident, _ in got:
+        assert np.array_equal(cl, ocl) and np.array_equal(ident, oid)
+
+
 def test_stepwise_equals_full(cuda_device):
     db = family_db(0, n=400, anc=8, seed=51)
     p = ngia.params_clamp(0, 0.85, 5, 0)
