@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-drivers", action="store_true", help="skip the whole-job graph vs plain comparison")
     ap.add_argument("--autotune", type=int, default=4, help="iterations per setting tried by ngia_autotune (0: off)")
+    ap.add_argument("--sweep", default="", help="comma-separated similarities to time as well (e.g. 0.8,0.85,0.9)")
+    ap.add_argument("--sweep-steps", type=int, default=3)
     ap.add_argument("--cpu-only", action="store_true",
                     help="replica plumbing with the CPU oracle as the engine (tests; no GPU)")
     return ap.parse_args()
@@ -298,6 +300,29 @@ def run_ours(args, dist: Dist):
                    "timing": "host clock around ngia_cluster (assignment and scores returned)"}
         sdb.close()
 
+    # similarity sweep of the same database (configuration 2 lists s = 0.80,
+    # 0.85, 0.90, 0.95, 0.99): tuned, then timed over a few steps each
+    sweep = None
+    if dist.rank == 0 and args.sweep:
+        sweep = []
+        for sv in (float(x) for x in args.sweep.split(",")):
+            sp = ngia.params_clamp(cfg["type"], sv, args.word, 0)
+            with ngia.Context(db) as sctx:
+                tun = sctx.autotune(sp, args.autotune) if args.autotune > 0 else None
+                sctx.begin(sp, ngia.MODE_GRAPH)
+                sctx.step(S)
+                a0 = sctx.stats()
+                ms = 0.0
+                for _ in range(args.sweep_steps):
+                    sctx.step(S)
+                    ms += sctx.step_ms()
+                a1 = sctx.stats()
+            sweep.append({"similarity": sv, "word_length": sp.word_length,
+                          "value": (a1["candidates"] - a0["candidates"]) / (ms * 1e-3),
+                          "gcups": (a1["band_cells"] - a0["band_cells"]) / (ms * 1e-3) / 1e9,
+                          "ms_per_iteration": ms / (args.sweep_steps * S),
+                          "tuning": {k: tun[k] for k in ("word_order", "refill", "warp_pairs")} if tun else None})
+
     out = None
     if dist.rank == 0:
         planes = 2 if cfg["type"] == 0 else 5
@@ -340,6 +365,7 @@ def run_ours(args, dist: Dist):
                "gpu_launches": launches_per_iter * S * args.steps,
                "drivers_whole_job": drivers,
                "tuning": tuning,
+               "similarity_sweep": sweep,
                "clocks": clk, "cpu_baseline": cpu, "e2e": e2e}
     db.close()
     if out is not None:
