@@ -325,8 +325,10 @@ def run_ours(args, dist: Dist):
 
     out = None
     if dist.rank == 0:
-        planes = 2 if cfg["type"] == 0 else 5
-        ops = planes + 2  # INT32 operations per 32-cell word step: one LOP3 per plane, add, LOP3
+        # INT32 operations per 32-cell word step: DNA reads the match word from
+        # the representative's match table (AND, add with carry, LOP3);
+        # protein builds it from 5 planes (one LOP3 per plane, add, LOP3)
+        ops = 3 if cfg["type"] == 0 else 7
         peak_gcell = int_gops * 32.0 / ops
         peaks = measured_peaks()
         e2e = None

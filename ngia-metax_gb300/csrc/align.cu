@@ -14,19 +14,22 @@
 // Two kernels reproduce that exactly:
 //
 // k_align_win<P,WC>  one thread per pair.  The band window (at most WC rep
-//   blocks) lives in registers: row[m] and the rep's planes pl[p][m] for
-//   slot m = rep block js+m.  For each query residue the whole window is
-//   updated as one multi-word addition whose carries ride the hardware carry
-//   flag (add.cc/addc.cc), i.e. four integer instructions per 32 cells for DNA
-//   (two LOP3 for the match mask, one IADD3.X, one LOP3 for the row).  When
-//   the band slides, the departing block's zero count is banked and the
-//   registers shift down one slot; an entering block starts all-ones.  Lanes
-//   claim pairs from the class queue independently (warp-aggregated atomics).
+//   blocks) lives in registers: row[m] for slot m = rep block js+m.  For each
+//   query residue the whole window is updated as one multi-word addition
+//   whose carries ride the hardware carry flag (add.cc/addc.cc).  The match
+//   word of a slot comes, for DNA, from the representative's match table in
+//   shared memory (four words per rep block, one per residue code; tile.cuh),
+//   so a 32-cell word costs one load and three integer instructions (AND,
+//   IADD3.X, LOP3); protein builds it from the rep's planes held in registers
+//   (one LOP3 per plane).  When the band slides, the departing block's zero
+//   count is banked and the registers shift down one slot; an entering block
+//   starts all-ones.  Lanes claim pairs from the class queue independently
+//   (warp-aggregated atomics).
 //
 // k_align_tiled<P,RING>  wider windows: one thread per pair, the band rows
 //   in a ring (shared memory for windows up to RING = 64 or 128 blocks,
 //   global scratch for any width with RING = 0), updated tile by tile with
-//   the same generated instruction sequence.
+//   the same generated instruction sequences.
 //
 // Both stop a pair early once it provably cannot reach the cutoff: each query
 // residue raises the counted zeros by at most one (the bit-vector update only
@@ -193,13 +196,19 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
   if (!align_setup<P>(db, rb, prm, cls, score_mode, warp_pairs, 0, smem, &bar, h)) return;
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
+  constexpr bool kEq = P == 2 && NGIA_WIN_EQ;
+  uint32_t *s_eq = smem + tiled_eq_off(P, db.max_nb, 0);
+  if constexpr (kEq) {
+    build_eq(s_pl, h.nb1, s_eq);  // the representative's match table (tile.cuh)
+    __syncthreads();
+  }
   RunState *st = rb.st;
   const int lane = threadIdx.x & 31;
   const float s = prm.s;
   const int nb1 = h.nb1;
   const uint32_t vlast = (h.net1 & 31) ? ((1u << (h.net1 & 31)) - 1u) : 0xFFFFFFFFu;
 
-  uint32_t row[WC], pl[P][WC], cur[P], nxt[P];
+  uint32_t row[WC], pl[kEq ? 1 : P][WC], cur[P], nxt[P];
   int state = -1, entry = 0, cand = 0;
   int i = 0, nq = 0, B = 0, js = 0, je = -1, net2 = 0, L2 = 0, cutoff = 0, lastcols = 32, frozen = 0;
   const uint32_t *qpl = nullptr;
@@ -237,8 +246,10 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
 #pragma unroll
       for (int m = 0; m < WC; m++) {
         row[m] = 0xFFFFFFFFu;
+        if constexpr (!kEq) {
 #pragma unroll
-        for (int p = 0; p < P; p++) pl[p][m] = (m <= je) ? s_pl[m * P + p] : 0u;
+          for (int p = 0; p < P; p++) pl[p][m] = (m <= je) ? s_pl[m * P + p] : 0u;
+        }
       }
 #pragma unroll
       for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
@@ -250,10 +261,19 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
 #pragma unroll
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
     }
+    uint32_t cw_unused = 0;
+    if constexpr (kEq) {
+      // match words of slot m for column k: s_eq[4 (js + m) + code_k]; slots
+      // past je read blocks not in the band (or the table's zero blocks):
+      // those rows are reset when they enter the band
+      uint32_t q[4];
+      eq_codes(cur, q);
+      const char *eb = reinterpret_cast<const char *>(s_eq + 4 * js);
+      eq_columns<WC, false, NGIA_EQ_PF_WIN>(row, eb, q, cols, cw_unused, cw_unused);
+    } else {
     uint32_t rv[P];
 #pragma unroll
     for (int p = 0; p < P; p++) rv[p] = __brev(cur[p]);
-    uint32_t cw_unused = 0;
     int k = 0;
     for (; k + 2 <= cols; k += 2) {
       uint32_t mk[P];
@@ -276,6 +296,7 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
       for (int p = 0; p < P; p++) mk[p] = (uint32_t)((int)rv[p] >> 31);
       dp_tile<P, WC, false, false>(row, pl, mk, cw_unused, cw_unused);
     }
+    }
     // ---- slide the band to query block i+1 --------------------------------
     i++;
     bool finished = i >= nq;
@@ -285,8 +306,10 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
 #pragma unroll
         for (int m = 0; m < WC - 1; m++) {
           row[m] = row[m + 1];
+          if constexpr (!kEq) {
 #pragma unroll
-          for (int p = 0; p < P; p++) pl[p][m] = pl[p][m + 1];
+            for (int p = 0; p < P; p++) pl[p][m] = pl[p][m + 1];
+          }
         }
         js++;
       }
@@ -295,13 +318,15 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
         const int slot = je - js;
         uint32_t v[P];
 #pragma unroll
-        for (int p = 0; p < P; p++) v[p] = s_pl[je * P + p];
+        for (int p = 0; p < P; p++) v[p] = kEq ? 0u : s_pl[je * P + p];
 #pragma unroll
         for (int m = 0; m < WC; m++)
           if (m == slot) {
             row[m] = 0xFFFFFFFFu;
+            if constexpr (!kEq) {
 #pragma unroll
-            for (int p = 0; p < P; p++) pl[p][m] = v[p];
+              for (int p = 0; p < P; p++) pl[p][m] = v[p];
+            }
           }
       }
       if (js > je) finished = true;  // band ran past the representative
@@ -361,6 +386,12 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
   RunState *st = rb.st;
+  constexpr bool kEq = P == 2 && NGIA_ALIGN_EQ;
+  uint32_t *s_eq = smem + tiled_eq_off(P, db.max_nb, RING);
+  if constexpr (kEq) {
+    build_eq(s_pl, h.nb1, s_eq);  // the representative's match table (tile.cuh)
+    __syncthreads();
+  }
   typename RingOf<RING>::T ring;
   if constexpr (RING > 0) {
     ring.base = smem + (((db.max_nb * P + 3) & ~3) + kListWords) + threadIdx.x;
@@ -443,7 +474,25 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 #pragma unroll
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
     }
-    {
+    if constexpr (kEq) {
+      rem = (rem + kEqRemRound - 1) / kEqRemRound * kEqRemRound;  // extra slots are padding
+      uint32_t q[4];
+      eq_codes(cur, q);
+      uint32_t cw = 0, ncw = 0;
+      int base = js;
+      for (int t = 0; t < full; t++, base += MT) {
+        zw += tiled_tile_eq<MT, NGIA_EQ_PF_MAIN, typename RingOf<RING>::T>(ring, s_eq, base, je, nb1, cols, q, cw, ncw);
+        cw = ncw << (32 - cols);  // column 0's carry at bit 31
+        ncw = 0;
+      }
+      for (; rem >= MT; rem -= MT, base += MT) {
+        zw += tiled_tile_eq<MT, NGIA_EQ_PF_MAIN, typename RingOf<RING>::T>(ring, s_eq, base, je, nb1, cols, q, cw, ncw);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      if (rem > 0)
+        zw += tiled_rem_eq<typename RingOf<RING>::T, MT>(rem, ring, s_eq, base, je, nb1, cols, q, cw, ncw);
+    } else {
       uint32_t cw = 0, ncw = 0;
       int base = js;
       for (int t = 0; t < full; t++, base += MT) {
@@ -724,7 +773,10 @@ static size_t align_smem(int type, int max_nb, int cls) {
   const int P = type ? 5 : 2;
   size_t words = (size_t)(((max_nb * P + 3) & ~3) + kListWords);
   if (cls == kWarpKernel) return 4u * (words + (size_t)(kAlignThreads / 32) * max_nb);
-  if (is_tiled_class(type, cls)) words += (size_t)class_cap(type, cls) * kAlignThreads;
+  const bool tiled = is_tiled_class(type, cls) || cls == generic_class(type);  // k_align_tiled
+  const int ring = tiled ? class_cap(type, cls) : 0;  // 64, 128, or 0 (global ring)
+  words = (size_t)tiled_eq_off(P, max_nb, ring);
+  if (P == 2 && (tiled ? NGIA_ALIGN_EQ : NGIA_WIN_EQ)) words += (size_t)eq_words(max_nb);
   return 4u * words;
 }
 

@@ -71,6 +71,53 @@ def one(P: int, TW: int, cin: bool, cout: bool) -> str:
             ");\n}\n")
 
 
+def one_eq(TW: int, cin: bool, cout: bool) -> str:
+    """DNA tile update from precomputed match words: e[m] is the match word of
+    slot m for the column's residue (read from the representative's match
+    table), so the match costs one AND instead of one LOP3 per plane:
+        x = row & e;  t = row + x + carry;  row = t | (row ^ x)
+    three integer instructions per 32 cells."""
+    outs = [f'"+r"(row[{m}])' for m in range(TW)]
+    idx_cw = idx_ncw = None
+    if cin:
+        idx_cw = len(outs)
+        outs.append('"+r"(cw)')
+    if cout:
+        idx_ncw = len(outs)
+        outs.append('"+r"(ncw)')
+    ins = []
+    e_idx = {}
+    for m in range(TW):
+        e_idx[m] = len(outs) + len(ins)
+        ins.append(f'"r"(e[{m}])')
+    lines = ["{", ".reg .u32 x, t;"]
+    if cin:
+        lines.append(f"add.cc.u32 %{idx_cw}, %{idx_cw}, %{idx_cw};")
+    for m in range(TW):
+        lines.append(f"and.b32 x, %{m}, %{e_idx[m]};")
+        first = (m == 0 and not cin)
+        last_no_out = (m == TW - 1 and not cout)
+        op = "add" if first else "addc"
+        cc = "" if last_no_out else ".cc"
+        lines.append(f"{op}{cc}.u32 t, %{m}, x;")
+        lines.append(f"lop3.b32 %{m}, t, %{m}, x, 0xF6;")
+    if cout:
+        lines.append(f"addc.u32 %{idx_ncw}, %{idx_ncw}, %{idx_ncw};")
+    lines.append("}")
+    body = "\n".join(f'      "{ln}\\n\\t"' for ln in lines)
+    sig = (f"template <>\n__device__ __forceinline__ void dp_tile_eq<{TW}, {str(cin).lower()}, "
+           f"{str(cout).lower()}>(uint32_t (&row)[{TW}], const uint32_t (&e)[{TW}], uint32_t &cw, "
+           f"uint32_t &ncw) {{\n")
+    unused = []
+    if not cin:
+        unused.append("cw")
+    if not cout:
+        unused.append("ncw")
+    void = "".join(f"  (void){u};\n" for u in unused)
+    return (sig + void + "  asm(\n" + body + "\n      : " + ", ".join(outs) + "\n      : " + ", ".join(ins) +
+            ");\n}\n")
+
+
 def main() -> None:
     parts = ["// dp_asm.cuh — generated by gen_dp_asm.py; do not edit by hand.\n"
              "// One residue (column) update of a TW-slot register tile of the banded\n"
@@ -78,12 +125,19 @@ def main() -> None:
              "#pragma once\n#include <stdint.h>\n\nnamespace ngia {\n\n"
              "template <int P, int TW, bool CIN, bool COUT>\n"
              "__device__ __forceinline__ void dp_tile(uint32_t (&row)[TW], const uint32_t (&pl)[P][TW],\n"
-             "                                        const uint32_t (&mk)[P], uint32_t &cw, uint32_t &ncw);\n\n"]
+             "                                        const uint32_t (&mk)[P], uint32_t &cw, uint32_t &ncw);\n\n"
+             "template <int TW, bool CIN, bool COUT>\n"
+             "__device__ __forceinline__ void dp_tile_eq(uint32_t (&row)[TW], const uint32_t (&e)[TW], uint32_t &cw,\n"
+             "                                           uint32_t &ncw);\n\n"]
     for P in PLANES:
         for TW in WIDTHS:
             for cin, cout in ((False, False), (True, True)):
                 parts.append(one(P, TW, cin, cout))
                 parts.append("\n")
+    for TW in WIDTHS:
+        for cin, cout in ((False, False), (True, True)):
+            parts.append(one_eq(TW, cin, cout))
+            parts.append("\n")
     parts.append("}  // namespace ngia\n")
     (Path(__file__).resolve().parent / "dp_asm.cuh").write_text("".join(parts))
 

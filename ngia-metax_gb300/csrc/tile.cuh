@@ -8,16 +8,47 @@
 #include "common.cuh"
 #include "dp_asm.cuh"
 
-// Build-time tuning of the tiled kernel: NGIA_TILED_MAIN_DNA and
-// NGIA_TILED_BLOCKS_DNA set the DNA main tile width and the resident CTAs per
-// SM requested from the register allocator.  On GB300 (1M DNA, s=0.85) 16
-// slots at 4 CTAs ran fastest: 24 slots (3 or 2 CTAs) and 32 slots (2 CTAs)
-// were 15-45% slower.
+// Build-time tuning of the DNA alignment kernels (swept on GB300, 1M DNA):
+//  NGIA_TILED_MAIN_DNA / NGIA_TILED_BLOCKS_DNA  main tile width and resident
+//    CTAs per SM of the tiled kernel: 16 slots at 4 CTAs.  24 and 32 slots,
+//    and 5 CTAs, were slower (the kernel is sensitive to its instruction
+//    footprint: wider tiles mean larger unrolled bodies).
+//  NGIA_ALIGN_EQ / NGIA_WIN_EQ  match words from the representative's match
+//    table (1) instead of from plane registers (0): 16% (tiled, s=0.85) and
+//    12-26% (window kernels, s=0.9-0.95) more candidate seqs/s.
+//  NGIA_EQ_UNROLL  columns per loop trip of the match-table tile: 1.  Two,
+//    four and eight ran at 0.92x, 0.64x and 0.41x: the larger bodies miss in
+//    the instruction cache.
+//  NGIA_EQ_PF_MAIN / NGIA_EQ_PF_WIN  load the next column's match words
+//    during the current column (eq_columns) in the main tiled tile / the
+//    window kernels: main on (+2% at s=0.85 and 0.9, -5% at 0.95), windows
+//    off (+30% for the 32-block window class alone at s=0.85-0.9, but slower
+//    at 0.95 and no faster overall).
+//  NGIA_EQ_REM_ROUND  remainder tiles rounded up to a multiple of this
+//    width (fewer tile variants, more padding slots): 1 (2 and 4 no faster).
 #ifndef NGIA_TILED_MAIN_DNA
 #define NGIA_TILED_MAIN_DNA 16
 #endif
 #ifndef NGIA_TILED_BLOCKS_DNA
 #define NGIA_TILED_BLOCKS_DNA 4
+#endif
+#ifndef NGIA_ALIGN_EQ
+#define NGIA_ALIGN_EQ 1
+#endif
+#ifndef NGIA_WIN_EQ
+#define NGIA_WIN_EQ 1
+#endif
+#ifndef NGIA_EQ_UNROLL
+#define NGIA_EQ_UNROLL 1
+#endif
+#ifndef NGIA_EQ_PF_MAIN
+#define NGIA_EQ_PF_MAIN 1
+#endif
+#ifndef NGIA_EQ_PF_WIN
+#define NGIA_EQ_PF_WIN 0
+#endif
+#ifndef NGIA_EQ_REM_ROUND
+#define NGIA_EQ_REM_ROUND 1
 #endif
 
 namespace ngia {
@@ -92,6 +123,158 @@ __device__ __forceinline__ int tiled_tile(const Ring &ring, const uint32_t *s_pl
     }
   }
   return znew - zold;
+}
+
+// DNA match table: for every rep block j its four match words, word 4j + c =
+// the rows of block j whose residue is c (c = plane-0 bit | plane-1 bit << 1),
+// i.e. ~(p0 ^ m0) & ~(p1 ^ m1) for the masks of residue c — the same words
+// the plane form builds per column.  kEqPad zero blocks follow the last rep
+// block, so a tile's padding slots (rows above je, whose row words are 0 and
+// mask whatever they read) stay inside the table.
+constexpr int kEqPad = 32;
+constexpr int kEqUnroll = NGIA_EQ_UNROLL;  // columns per loop trip of tiled_tile_eq
+__host__ __device__ constexpr int eq_words(int max_nb) { return 4 * (max_nb + kEqPad); }
+// Word offset of the match table in the tiled kernel's dynamic shared memory:
+// after the planes, the k-mer bitset and the row ring (ring = 0: global ring).
+__host__ __device__ constexpr int tiled_eq_off(int P, int max_nb, int ring) {
+  return ((max_nb * P + 3) & ~3) + kListWords + ring * kAlignThreads;
+}
+
+// Builds the match table of the representative whose planes are staged at
+// s_pl (nb1 blocks) with all threads of the CTA; the caller synchronises.
+__device__ __forceinline__ void build_eq(const uint32_t *s_pl, int nb1, uint32_t *s_eq) {
+  for (int j = threadIdx.x; j < nb1 + kEqPad; j += blockDim.x) {
+    const bool real = j < nb1;
+    const uint32_t p0 = real ? s_pl[2 * j] : 0u, p1 = real ? s_pl[2 * j + 1] : 0u;
+    uint4 e;
+    e.x = real ? ~p0 & ~p1 : 0u;
+    e.y = p0 & ~p1;
+    e.z = ~p0 & p1;
+    e.w = p0 & p1;
+    *reinterpret_cast<uint4 *>(s_eq + 4 * j) = e;
+  }
+}
+
+// Column codes of one 32-residue query block as byte offsets into a block's
+// four match words: column k's offset 4c sits in bits 4(k%8)..4(k%8)+3 of
+// q[k/8].
+__device__ __forceinline__ void eq_codes(const uint32_t (&cur)[2], uint32_t (&q)[4]) {
+#pragma unroll
+  for (int s = 0; s < 4; s++) {
+    uint32_t a = (cur[0] >> (8 * s)) & 0xFFu, b = (cur[1] >> (8 * s)) & 0xFFu;
+    a = (a | (a << 12)) & 0x000F000Fu;
+    a = (a | (a << 6)) & 0x03030303u;
+    a = (a | (a << 3)) & 0x11111111u;
+    b = (b | (b << 12)) & 0x000F000Fu;
+    b = (b | (b << 6)) & 0x03030303u;
+    b = (b | (b << 3)) & 0x11111111u;
+    q[s] = (a << 2) | (b << 3);
+  }
+}
+
+// Match words of the TW slots at eb (block-major table, byte offset `off`
+// selects the residue's word of each block).
+template <int TW>
+__device__ __forceinline__ void eq_load(uint32_t (&e)[TW], const char *eb, uint32_t off) {
+  const uint32_t *p = reinterpret_cast<const uint32_t *>(eb + off);
+#pragma unroll
+  for (int m = 0; m < TW; m++) e[m] = p[4 * m];
+}
+
+// All `cols` columns of one query block through a register tile of TW
+// slots whose match words start at eb; CC: the tile takes column carries in
+// cw and hands them out in ncw.  PF: the next column's match words are loaded
+// while the current column updates (two columns per loop trip), hiding the
+// shared-memory latency behind the carry chain; loads past the last column
+// read offset 0 (in bounds, unused).
+template <int TW, bool CC, bool PF>
+__device__ __forceinline__ void eq_columns(uint32_t (&row)[TW], const char *eb, const uint32_t (&q)[4], int cols,
+                                           uint32_t &cw, uint32_t &ncw) {
+  uint32_t w0 = q[0], w1 = q[1], w2 = q[2], w3 = q[3];
+  for (int k0 = 0; k0 < cols; k0 += 8) {
+    uint32_t w = w0;
+    w0 = w1;
+    w1 = w2;
+    w2 = w3;
+    const int n = min(8, cols - k0);
+    if constexpr (PF) {
+      uint32_t ea[TW], eo[TW];
+      eq_load<TW>(ea, eb, w & 12u);
+      w >>= 4;
+      int k = 0;
+#pragma unroll 1
+      for (; k + 2 <= n; k += 2) {
+        eq_load<TW>(eo, eb, w & 12u);
+        w >>= 4;
+        dp_tile_eq<TW, CC, CC>(row, ea, cw, ncw);
+        eq_load<TW>(ea, eb, w & 12u);
+        w >>= 4;
+        dp_tile_eq<TW, CC, CC>(row, eo, cw, ncw);
+      }
+      if (k < n) dp_tile_eq<TW, CC, CC>(row, ea, cw, ncw);
+    } else {
+#pragma unroll kEqUnroll
+      for (int k = 0; k < n; k++) {
+        uint32_t ev[TW];
+        eq_load<TW>(ev, eb, w & 12u);
+        w >>= 4;
+        dp_tile_eq<TW, CC, CC>(row, ev, cw, ncw);
+      }
+    }
+  }
+}
+
+// tiled_tile for DNA with the match table: per column one shared-memory load
+// per slot and three integer instructions per 32 cells (AND, add with carry,
+// LOP3) instead of four.  s_eq points at the table; q holds the column codes.
+template <int TW, bool PF, class Ring>
+__device__ __forceinline__ int tiled_tile_eq(const Ring &ring, const uint32_t *s_eq, int base, int je, int nb1,
+                                             int cols, const uint32_t (&q)[4], uint32_t &cw, uint32_t &ncw) {
+  uint32_t row[TW];
+  int zold = 0;
+#pragma unroll
+  for (int m = 0; m < TW; m++) {
+    const int j = base + m;
+    const bool in = j <= je;
+    row[m] = in ? ring[j] : 0u;
+    zold += in ? __popc(~row[m]) : 0;
+  }
+  // A tile past the rep's last block (a lane with a narrower window than its
+  // warp's widest) is all padding: it reads the zero blocks after nb1.
+  const char *eb = reinterpret_cast<const char *>(s_eq + 4 * min(base, nb1));
+  eq_columns<TW, true, PF>(row, eb, q, cols, cw, ncw);
+  int znew = 0;
+#pragma unroll
+  for (int m = 0; m < TW; m++) {
+    const int j = base + m;
+    if (j <= je) {
+      ring[j] = row[m];
+      znew += __popc(~row[m]);
+    }
+  }
+  return znew - zold;
+}
+
+constexpr int kEqRemRound = NGIA_EQ_REM_ROUND;  // remainder tile widths: multiples of this
+
+template <class Ring, int MT>
+__device__ __forceinline__ int tiled_rem_eq(int rem, const Ring &ring, const uint32_t *s_eq, int base, int je,
+                                            int nb1, int cols, const uint32_t (&q)[4], uint32_t &cw, uint32_t &ncw) {
+  switch (rem) {
+#define NGIA_REM(W) \
+  case W:           \
+    if (W < MT && W % kEqRemRound == 0)                                                                     \
+      return tiled_tile_eq<(W < MT && W % kEqRemRound == 0 ? W : kEqRemRound), false, Ring>(ring, s_eq, base, je, nb1,  \
+                                                                                     cols, q, cw, ncw);         \
+    return 0;
+    NGIA_REM(1) NGIA_REM(2) NGIA_REM(3) NGIA_REM(4) NGIA_REM(5) NGIA_REM(6) NGIA_REM(7) NGIA_REM(8)
+    NGIA_REM(9) NGIA_REM(10) NGIA_REM(11) NGIA_REM(12) NGIA_REM(13) NGIA_REM(14) NGIA_REM(15) NGIA_REM(16)
+    NGIA_REM(17) NGIA_REM(18) NGIA_REM(19) NGIA_REM(20) NGIA_REM(21) NGIA_REM(22) NGIA_REM(23) NGIA_REM(24)
+    NGIA_REM(25) NGIA_REM(26) NGIA_REM(27) NGIA_REM(28) NGIA_REM(29) NGIA_REM(30) NGIA_REM(31)
+#undef NGIA_REM
+    default:
+      return 0;
+  }
 }
 
 // The last tile of a block row, exactly `rem` (1..MT-1, warp-uniform) slots wide.
