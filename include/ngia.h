@@ -138,6 +138,18 @@ typedef struct ngia_ctx ngia_ctx;
 #define NGIA_MODE_PLAIN  0  /* host loop: one launch sequence per representative */
 #define NGIA_MODE_GRAPH  1  /* device-side driver in a captured CUDA graph
                                (conditional while node), no host round trip  */
+#define NGIA_MODE_SPEC   2  /* speculative rounds once the unclustered set is
+                               small (<= 262,144 sequences): the next K of them
+                               are candidate representatives of one round,
+                               every pair against them runs at once and the
+                               greedy order is replayed on the device (same
+                               result as the one-representative loop); host
+                               loop per round.  Plain iterations while the
+                               set is larger, and throughout when the database
+                               has records of net length < 16 and precise is
+                               0 (the reference's short-word kernel then makes
+                               a pair's test depend on its iteration's job
+                               list).                                        */
 
 typedef struct ngia_stats {
     int64_t iterations;    /* representatives taken (= clusters)             */

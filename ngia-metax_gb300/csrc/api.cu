@@ -100,6 +100,12 @@ void fill_stats(const ngia_ctx *c, ngia_stats *stats) {
   stats->filter_bytes = (int64_t)s.st_filter_bytes;
   stats->word_checks = (int64_t)s.st_word_checks;
   stats->done_cells = (int64_t)s.st_done_cells;
+  if (c->mode == NGIA_MODE_SPEC) {  // pairs and cells of the speculative rounds
+    int64_t pairs = 0, cells = 0;
+    spec_stats(c, &pairs, &cells);
+    stats->align_pairs += pairs;
+    stats->done_cells += cells;
+  }
   stats->ms_filter = c->ms_filter;
   stats->ms_align = c->ms_align;
   for (int k = 0; k < 8; k++) {
@@ -411,6 +417,7 @@ extern "C" int ngia_close(ngia_ctx *c) {
   if (!c) return NGIA_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
   destroy_graph(c);
+  ngia::drv::spec_free(c);
   cudaFree(c->d_words);
   cudaFree(c->d_off);
   cudaFree(c->d_len);
@@ -466,7 +473,8 @@ int ngia::drv::begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, con
   if (c->db.n <= 0) return fail(NGIA_E_STATE, "ngia_cluster_begin: no database loaded");
   int rc = validate_params(c->db.type, p);
   if (rc) return rc;
-  if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH) return fail(NGIA_E_ARG, "unknown mode %d", mode);
+  if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH && mode != NGIA_MODE_SPEC)
+    return fail(NGIA_E_ARG, "unknown mode %d", mode);
   c->prm.s = p->similarity;
   c->prm.w = p->word_length;
   c->prm.precise = p->precise;
@@ -489,6 +497,10 @@ int ngia::drv::begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, con
     rc = build_graph(c);
     if (rc) return rc;
   }
+  if (mode == NGIA_MODE_SPEC) {
+    rc = spec_prepare(c);
+    if (rc) return rc;
+  }
   c->begun = true;
   return NGIA_OK;
 }
@@ -509,6 +521,12 @@ extern "C" int ngia_cluster_step(ngia_ctx *c, int64_t max_iters, int32_t *done) 
     CK(cudaEventRecord(c->ev_step1, c->stream));
     int rc = pull_state(c);
     if (rc) return rc;
+  } else if (c->mode == NGIA_MODE_SPEC) {
+    CK(cudaEventRecord(c->ev_step0, c->stream));
+    int rc = ngia::drv::spec_step(c, max_iters);
+    if (rc) return rc;
+    CK(cudaEventRecord(c->ev_step1, c->stream));
+    CK(cudaEventSynchronize(c->ev_step1));
   } else {
     CK(cudaEventRecord(c->ev_step0, c->stream));
     for (int64_t it = 0; max_iters <= 0 || it < max_iters; it++) {

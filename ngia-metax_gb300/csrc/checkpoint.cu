@@ -128,7 +128,8 @@ extern "C" int ngia_cluster_save(ngia_ctx *c, const char *path) {
 extern "C" int ngia_cluster_resume(ngia_ctx *c, const char *path, int32_t mode) {
   ngia::clear_error();
   if (!c || !path) return fail(NGIA_E_ARG, "ngia_cluster_resume: null argument");
-  if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH) return fail(NGIA_E_ARG, "unknown mode %d", mode);
+  if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH && mode != NGIA_MODE_SPEC)
+    return fail(NGIA_E_ARG, "unknown mode %d", mode);
   FILE *f = fopen(path, "rb");
   if (!f) return fail(NGIA_E_IO, "ngia_cluster_resume: cannot open %s", path);
   CkptHeader h{};
@@ -180,6 +181,10 @@ extern "C" int ngia_cluster_resume(ngia_ctx *c, const char *path, int32_t mode) 
   if (mode == NGIA_MODE_GRAPH) {
     ngia::drv::destroy_graph(c);
     rc = ngia::drv::build_graph(c);
+    if (rc) return rc;
+  }
+  if (mode == NGIA_MODE_SPEC) {
+    rc = ngia::drv::spec_prepare(c);
     if (rc) return rc;
   }
   c->begun = true;

@@ -6,6 +6,8 @@
 #include "../../include/ngia.h"
 #include "common.cuh"
 
+struct ngia_spec;  // speculative-round driver state (spec.cu)
+
 struct ngia_ctx {
   int device = 0;
   int num_sms = 0;
@@ -55,6 +57,7 @@ struct ngia_ctx {
   bool batch_member = false;  // grids sized to the job; serial class launches
   double ms_filter = 0.0, ms_align = 0.0, ms_class[ngia::kNumClasses] = {0.0};
   float last_step_ms = 0.f;
+  ngia_spec *spec = nullptr;  // NGIA_MODE_SPEC buffers, allocated on first use
 };
 
 namespace ngia {
@@ -77,6 +80,12 @@ int pull_state(ngia_ctx *c);
 int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond);
 void fill_stats(const ngia_ctx *c, ngia_stats *stats);
 int validate_params(int type, const ngia_params *p);
+// spec.cu: speculative rounds (NGIA_MODE_SPEC)
+int spec_prepare(ngia_ctx *c);                 // buffers for the context's capacity; zeroed masks
+int spec_step(ngia_ctx *c, int64_t max_iters);  // up to max_iters representatives (<= 0: all)
+void spec_free(ngia_ctx *c);
+bool spec_exact(const ngia_ctx *c);            // rounds reproduce the greedy loop exactly
+void spec_stats(const ngia_ctx *c, int64_t *pairs, int64_t *cells);
 }  // namespace drv
 // loader.cu / filter.cu
 cudaError_t launch_loader(ngia_ctx *c, int32_t *d_maxnb, int32_t *d_short, int32_t *d_bad);

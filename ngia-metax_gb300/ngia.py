@@ -17,6 +17,7 @@ LIB_PATH = HERE / "_build" / "libngia.so"
 
 MODE_PLAIN = 0
 MODE_GRAPH = 1
+MODE_SPEC = 2
 
 
 class NgiaError(RuntimeError):

@@ -345,3 +345,59 @@ def test_cli_flags():
     r = subprocess.run([exe, "-i", "/nonexistent", "-o", "y", "-w", "5", "-s", "0.9"], capture_output=True,
                        text=True)
     assert r.returncode == 2 and "data.bin" in r.stderr
+
+
+def _replay_rounds(db, p, k):
+    """The speculative rounds of the spec driver restated on the CPU with the
+    oracle's per-pair tests: the next k unclustered sequences are candidate
+    representatives; c_i is a representative iff no earlier representative
+    of the round accepts it; every sequence joins the first representative of
+    the round that accepts it."""
+    alive = np.ones(db.n, bool)
+    cl = np.full(db.n, -1, np.int32)
+    idn = np.full(db.n, -1, np.int32)
+    reps = 0
+    memo = {}
+
+    def test(r, x):
+        if (r, x) not in memo:
+            o = oracle.pair(db.words, db.rec_off, db.type, p.similarity, p.word_length, int(r), int(x))
+            short = db.words[db.rec_off[r] + 1] < 16 or db.words[db.rec_off[x] + 1] < 16
+            memo[(r, x)] = (bool(o[4]) and (bool(p.precise) or short or bool(o[5])) and bool(o[6]), int(o[2]))
+        return memo[(r, x)]
+
+    while alive.any():
+        idx = np.flatnonzero(alive)
+        cand = idx[:k]
+        acc = {}
+        for i, c in enumerate(cand):
+            for x in idx[idx >= c]:
+                ok, sc = test(c, x)
+                if ok:
+                    acc.setdefault(int(x), {})[i] = sc
+        valid = []
+        for i, c in enumerate(cand):
+            if not any(j in acc.get(int(c), {}) for j in valid):
+                valid.append(i)
+        reps += len(valid)
+        for x in idx:
+            a = acc.get(int(x), {})
+            hit = np.flatnonzero(cand == x)
+            if hit.size and int(hit[0]) in valid:
+                cl[x], idn[x], alive[x] = x, a.get(int(hit[0]), -1), False
+                continue
+            js = [j for j in valid if j in a]
+            if js:
+                cl[x], idn[x], alive[x] = cand[js[0]], a[js[0]], False
+    return cl, idn, reps
+
+
+@pytest.mark.parametrize("db_type,s,w,k", [(0, 0.85, 5, 4), (0, 0.85, 5, 64), (0, 0.95, 5, 16), (1, 0.5, 2, 64)])
+def test_speculative_rounds_replay_the_greedy_loop(db_type, s, w, k):
+    """The round resolution of the spec driver (csrc/spec.cu) gives the
+    greedy loop's clustering exactly, whatever the round size."""
+    db = family_db(db_type, n=120, anc=5, seed=3 + db_type)
+    p = ngia.params_clamp(db_type, s, w, 0)
+    ocl, oid, ost = oracle.cluster(db.words, db.rec_off, db_type, p.similarity, p.word_length, p.precise)
+    cl, idn, reps = _replay_rounds(db, p, k)
+    assert np.array_equal(cl, ocl) and np.array_equal(idn, oid) and reps == ost["iterations"]
