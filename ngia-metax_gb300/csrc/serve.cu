@@ -446,6 +446,7 @@ extern "C" int ngia_serve_open(const ngia_db_view *reps, const ngia_params *para
   sv->prm.w = params->word_length;
   sv->prm.precise = params->precise;
   sv->prm.word_order = 0;
+  if (const char *wo = getenv("NGIA_SERVE_WORD_ORDER")) sv->prm.word_order = std::max(0, std::min(2, atoi(wo)));
   sv->prm.refill = 32;
   sv->word_first = ngia::word_first_of(sv->type, sv->prm);
   sv->cap_n = cf.max_batch;

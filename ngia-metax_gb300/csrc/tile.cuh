@@ -24,6 +24,8 @@
 //    window kernels: main on (+2% at s=0.85 and 0.9, -5% at 0.95), windows
 //    off (+30% for the 32-block window class alone at s=0.85-0.9, but slower
 //    at 0.95 and no faster overall).
+//  (Running the last main tile and the remainder as one tile of 17-31 slots,
+//  to save a tile's per-column overhead, ran at 0.45x.)
 //  NGIA_EQ_REM_ROUND  remainder tiles rounded up to a multiple of this
 //    width (fewer tile variants, more padding slots): 1 (2 and 4 no faster).
 #ifndef NGIA_TILED_MAIN_DNA
