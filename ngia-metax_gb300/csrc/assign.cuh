@@ -27,7 +27,32 @@ struct RepStore {
   const uint32_t *lists;  // n x list_words k-mer bitsets (empty when net < 16)
   int32_t n, list_words;
   const int32_t *count;   // when set: the representatives in use (on the device, <= n)
+  const uint32_t *eq;     // DNA: match table of representative r at r * eq_stride (tile.cuh layout)
+  int64_t eq_stride;      // words per table: 4 x (largest plane blocks + kEqPad)
 };
+
+// DNA match tables (tile.cuh) of the representatives, one CTA each: four
+// words per plane block, zero from the representative's last block to the
+// end of its table.
+__global__ void k_rep_eq(RepStore rs, uint32_t *eq) {
+  const int r = blockIdx.x;
+  if (rs.count && r >= *rs.count) return;
+  const uint32_t *rec = rs.words + rs.off[r];
+  const int nb1 = ((int)rec[1] + 31) / 32;
+  const uint32_t *pl = rec + 6;  // DNA header words
+  uint4 *t = reinterpret_cast<uint4 *>(eq + (int64_t)r * rs.eq_stride);
+  const int blocks = (int)(rs.eq_stride / 4);
+  for (int j = threadIdx.x; j < blocks; j += blockDim.x) {
+    const bool real = j < nb1;
+    const uint32_t p0 = real ? pl[2 * j] : 0u, p1 = real ? pl[2 * j + 1] : 0u;
+    uint4 e;
+    e.x = real ? ~p0 & ~p1 : 0u;
+    e.y = p0 & ~p1;
+    e.z = ~p0 & p1;
+    e.w = p0 & p1;
+    t[j] = e;
+  }
+}
 
 // Buffers of the assignment rounds of one slot.
 struct RoundBufs {
@@ -255,7 +280,25 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 #pragma unroll
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
     }
-    {
+    if constexpr (P == 2 && NGIA_SERVE_EQ) {  // match words from the pair's representative's table
+      using Ring = typename RingOf<RING>::T;
+      const uint32_t *req = rs.eq + (int64_t)r * rs.eq_stride;
+      uint32_t q[4];
+      eq_codes(cur, q);
+      uint32_t cw = 0, ncw = 0;
+      int base = js;
+      for (int t = 0; t < full; t++, base += MT) {
+        zw += tiled_tile_eq<MT, NGIA_EQ_PF_MAIN, Ring>(ring, req, base, je, nb1, cols, q, cw, ncw);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      for (; rem >= MT; rem -= MT, base += MT) {
+        zw += tiled_tile_eq<MT, NGIA_EQ_PF_MAIN, Ring>(ring, req, base, je, nb1, cols, q, cw, ncw);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      if (rem > 0) zw += tiled_rem_eq<Ring, MT>(rem, ring, req, base, je, nb1, cols, q, cw, ncw);
+    } else {
       using Ring = typename RingOf<RING>::T;
       uint32_t cw = 0, ncw = 0;
       int base = js;

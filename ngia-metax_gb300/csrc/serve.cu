@@ -160,6 +160,7 @@ struct ngia_server {
   int word_first = 0;
   ngia_ctx *reps = nullptr;  // the resident representatives' database
   uint32_t *d_lists = nullptr;
+  uint32_t *d_eq = nullptr;  // DNA match tables of the representatives
   ngia::RepStore store{};
   int64_t cap_n = 0, cap_words = 0;
   int32_t cap_nb = 0;
@@ -404,6 +405,7 @@ void destroy(ngia_server *sv) {
   for (auto &sl : sv->slots) free_slot(*sl);
   if (sv->reps) ngia_close(sv->reps);
   cudaFree(sv->d_lists);
+  cudaFree(sv->d_eq);
   delete sv;
 }
 
@@ -467,10 +469,18 @@ extern "C" int ngia_serve_open(const ngia_db_view *reps, const ngia_params *para
   }
   sv->store = ngia::RepStore{rc_ctx->db.words, rc_ctx->db.off, rc_ctx->db.len, rc_ctx->db.net, rc_ctx->db.cnt,
                              sv->d_lists, rc_ctx->db.n, lw};
-  if (sv->type == 0)
+  if (sv->type == 0) {
+    sv->store.eq_stride = (int64_t)ngia::eq_words(rc_ctx->db.max_nb);
+    if (cudaMalloc((void **)&sv->d_eq, 4 * (size_t)sv->store.eq_stride * (size_t)reps->n) != cudaSuccess) {
+      ngia::destroy(sv);
+      return fail(NGIA_E_NOMEM, "ngia_serve_open: match table allocation failed");
+    }
+    sv->store.eq = sv->d_eq;
+    ngia::k_rep_eq<<<reps->n, 256, 0, rc_ctx->stream>>>(sv->store, sv->d_eq);
     ngia::k_rep_lists<2><<<reps->n, 256, 0, rc_ctx->stream>>>(sv->store, params->word_length, sv->d_lists);
-  else
+  } else {
     ngia::k_rep_lists<5><<<reps->n, 256, 0, rc_ctx->stream>>>(sv->store, params->word_length, sv->d_lists);
+  }
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaStreamSynchronize(rc_ctx->stream);
   if (e != cudaSuccess) {

@@ -61,6 +61,7 @@ struct SpecDev {
   SpecCtl *ctl;
   int64_t *rs_off;          // record offsets of the candidates (the RepStore's off)
   uint32_t *lists;          // k-mer bitsets of the candidates
+  uint32_t *eq;             // DNA match tables of the candidates
 };
 
 __device__ __forceinline__ int block_sum_1024(int v, int *s_red) {
@@ -311,6 +312,7 @@ struct ngia_spec {
   uint32_t *scratch = nullptr;
   int64_t scratch_words = 0;
   uint32_t ring_mask = 0;
+  int64_t eq_stride = 0;      // words per candidate match table
   int grid[ngia::kServeClasses] = {0, 0, 0};
   int budget = ngia::kSpecBudget;  // pairs per round (NGIA_SPEC_BUDGET lowers it)
   bool big = false;           // the unclustered set was above the round budget at the last check
@@ -338,7 +340,10 @@ constexpr size_t kCtlBytes = 8 * sizeof(uint32_t) + sizeof(SpecCtl);
 int spec_alloc(ngia_ctx *c) {
   ngia_spec *sp = c->spec;
   const int64_t n = std::max<int64_t>(c->cap_n, c->db.n);
-  if (sp && sp->cap_n >= n && sp->type == c->db.type && sp->ring_mask == c->rb.ring_mask) return NGIA_OK;
+  const int64_t eq_stride = (int64_t)eq_words(std::max(c->cap_nb, c->db.max_nb));
+  if (sp && sp->cap_n >= n && sp->type == c->db.type && sp->ring_mask == c->rb.ring_mask &&
+      sp->eq_stride >= eq_stride)
+    return NGIA_OK;
   spec_free(c);
   sp = new (std::nothrow) ngia_spec();
   if (!sp) return fail(NGIA_E_NOMEM, "spec: out of host memory");
@@ -347,9 +352,11 @@ int spec_alloc(ngia_ctx *c) {
   sp->type = c->db.type;
   sp->k_max = (int)std::max<int64_t>(1, std::min<int64_t>(kSpecMax, kSpecScoreWords / std::max<int64_t>(1, n)));
   sp->ring_mask = c->rb.ring_mask;
+  sp->eq_stride = eq_stride;
   const int lw = kListWords;
   if (dmalloc(&sp->d.c, kSpecMax) != cudaSuccess || dmalloc(&sp->d.rs_off, kSpecMax) != cudaSuccess ||
       dmalloc(&sp->d.lists, (size_t)kSpecMax * lw) != cudaSuccess || dmalloc(&sp->d_ctl, kCtlBytes) != cudaSuccess ||
+      dmalloc(&sp->d.eq, (size_t)kSpecMax * (size_t)eq_stride) != cudaSuccess ||
       cudaMallocHost((void **)&sp->h_ctl, kCtlBytes) != cudaSuccess ||
       dmalloc(&sp->rb.mask, (size_t)n) != cudaSuccess ||
       dmalloc(&sp->rb.score, (size_t)sp->k_max * (size_t)n) != cudaSuccess ||
@@ -389,7 +396,12 @@ int spec_launch_round(ngia_ctx *c, bool lists) {
   cudaStream_t st = c->stream;
   const int P = c->db.type ? 5 : 2;
   const int lw = (int)std::max<uint32_t>(1u, (1u << (c->prm.w * (P == 2 ? 2 : 5))) / 32u);
-  RepStore rs{c->db.words, sp->d.rs_off, nullptr, nullptr, nullptr, sp->d.lists, kSpecMax, lw, &sp->d.ctl->k};
+  RepStore rs{c->db.words, sp->d.rs_off, nullptr, nullptr,     nullptr, sp->d.lists,
+              kSpecMax,    lw,           &sp->d.ctl->k, sp->d.eq, sp->eq_stride};
+  if (P == 2) {
+    k_rep_eq<<<sp->k_max, 256, 0, st>>>(rs, sp->d.eq);
+    CKP(cudaGetLastError());
+  }
   if (lists) {
     if (P == 2)
       k_rep_lists<2><<<sp->k_max, 256, 0, st>>>(rs, c->prm.w, sp->d.lists);
@@ -456,6 +468,7 @@ void spec_free(ngia_ctx *c) {
   cudaFree(sp->d.c);
   cudaFree(sp->d.rs_off);
   cudaFree(sp->d.lists);
+  cudaFree(sp->d.eq);
   cudaFree(sp->d_ctl);
   if (sp->h_ctl) cudaFreeHost(sp->h_ctl);
   cudaFree(sp->rb.mask);

@@ -40,6 +40,9 @@
 #ifndef NGIA_WIN_EQ
 #define NGIA_WIN_EQ 1
 #endif
+#ifndef NGIA_SERVE_EQ
+#define NGIA_SERVE_EQ 1
+#endif
 #ifndef NGIA_EQ_UNROLL
 #define NGIA_EQ_UNROLL 1
 #endif
