@@ -3,7 +3,9 @@
 //   cluster -i <dbdir> -o <outdir> -w <word> -s <similarity> [-p 0|1]
 // reads <dbdir>/data.bin + data.fasta, clusters on the GPU through the C ABI
 // and writes <outdir>/cluster.txt and <outdir>/represent.fasta.
-// Environment: NGIA_MODE=plain|graph (default graph) selects the driver form;
+// Environment: NGIA_MODE=spec|graph|plain (default spec: plain iterations
+// while the unclustered set is large, speculative rounds once it is small)
+// selects the driver form;
 // NGIA_IDENTITY=<path> also writes "index<TAB>representative<TAB>score" lines.
 #include <algorithm>
 #include <chrono>
@@ -69,9 +71,11 @@ int main(int argc, char **argv) {
   tread.print();
   std::cout << std::endl;
 
-  int mode = NGIA_MODE_GRAPH;
-  if (const char *m = std::getenv("NGIA_MODE"))
+  int mode = NGIA_MODE_SPEC;
+  if (const char *m = std::getenv("NGIA_MODE")) {
     if (!std::strcmp(m, "plain")) mode = NGIA_MODE_PLAIN;
+    if (!std::strcmp(m, "graph")) mode = NGIA_MODE_GRAPH;
+  }
   ngia_ctx *ctx = nullptr;
   rc = ngia_open(&db->view, &ctx);
   if (rc) die("ngia_open", rc);
