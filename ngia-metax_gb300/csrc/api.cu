@@ -296,7 +296,7 @@ int alloc_run(ngia_ctx *c, int64_t cap_n, int cap_nb) {
             dalloc(&rb.rep_rec, 32 + (size_t)ngia::kMaxBlocks * 5 + 64) == cudaSuccess &&
             dalloc(&rb.rep_list, ngia::kListWords) == cudaSuccess &&
             dalloc(&rb.first_short, ngia::kRefGridThreads) == cudaSuccess &&
-            dalloc(&rb.scan_part, nbw) == cudaSuccess;
+            dalloc(&rb.scan_part, nbw) == cudaSuccess && dalloc(&rb.long_list, (size_t)cap_n) == cudaSuccess;
   ok = ok && cudaMalloc((void **)&rb.flags, 4 * std::max<size_t>(nbw, 1)) == cudaSuccess;
   ok = ok && dalloc(&rb.fstats, (size_t)ngia::kFilterStripes * ngia::kFilterStats) == cudaSuccess;
   for (int k = 0; ok && k < ngia::num_classes(type); k++) ok = dalloc(&rb.queue[k], (size_t)cap_n) == cudaSuccess;
@@ -432,6 +432,7 @@ extern "C" int ngia_close(ngia_ctx *c) {
   cudaFree(rb.rep_list);
   cudaFree(rb.first_short);
   cudaFree(rb.scan_part);
+  cudaFree(rb.long_list);
   cudaFree(rb.flags);
   cudaFree(rb.fstats);
   cudaFree(rb.scratch);

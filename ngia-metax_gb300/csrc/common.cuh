@@ -67,6 +67,7 @@ struct RunState {
   int64_t iter_limit;     // graph loop stops when iter reaches it
   uint32_t qcount[kNumClasses];  // pairs queued per class this iteration
   uint32_t qhead[kNumClasses];   // pairs claimed per class
+  uint32_t long_count;    // candidates left for k_filter_long this iteration
   int32_t word_first;     // 1: short-word filter before alignment
   int32_t word_active;    // 1: short-word filter applies this iteration
   int32_t rep_nb;         // plane blocks of the representative (net)
@@ -110,6 +111,7 @@ struct RunBufs {
   int32_t *pos;           // position of a base survivor in the job list
   int32_t *first_short;   // per reference thread: first job with net < 16
   uint32_t *scan_part;    // scan partials
+  int32_t *long_list;     // candidates whose short-word count k_filter_long takes (one warp each)
   uint32_t *scratch;      // per-lane band rows of the widest class (global ring)
   int64_t scratch_words;
   int32_t generic_lanes;

@@ -80,6 +80,7 @@ __global__ void k_init_run(DevDB db, RunBufs rb, RunParams prm) {
     st->iter = 0;
     st->iter_limit = LLONG_MAX;
     for (int k = 0; k < kNumClasses; k++) st->qcount[k] = st->qhead[k] = 0;
+    st->long_count = 0;
     st->word_first = word_first_of(db.type, prm);
     st->word_active = 0;
     st->rep_nb = st->rep_len = st->rep_net = 0;
@@ -114,8 +115,10 @@ __global__ void k_prep(DevDB db, RunBufs rb, RunParams prm, int score_rep) {
   }
   __syncthreads();
   if (s_skip) {  // loop finished: nothing queued for the kernels after this one
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
       for (int k = 0; k < kNumClasses; k++) st->qcount[k] = st->qhead[k] = 0;
+      st->long_count = 0;
+    }
     return;
   }
   const int r = score_rep >= 0 ? score_rep : st->rep;
@@ -151,6 +154,7 @@ __global__ void k_prep(DevDB db, RunBufs rb, RunParams prm, int score_rep) {
     st->rep_nb = nb1;
     st->word_active = word_active;
     for (int k = 0; k < kNumClasses; k++) st->qcount[k] = st->qhead[k] = 0;
+    st->long_count = 0;
     if (score_rep < 0) {
       rb.cluster[r] = r;  // updateRepresent marks the representative (func.cu:235)
       rb.ident[r] = -1;
@@ -423,6 +427,11 @@ __device__ __forceinline__ void flush_stats(const RunBufs &rb, unsigned long lon
 #ifndef NGIA_FILTER_WPW_WORD
 #define NGIA_FILTER_WPW_WORD 1
 #endif
+// NGIA_FILTER_WARP_WORD: with the short-word test in the filter, warps take
+// bitmap words independently (no tile barriers); 0 keeps the tiled loop.
+#ifndef NGIA_FILTER_WARP_WORD
+#define NGIA_FILTER_WARP_WORD 1
+#endif
 
 template <int P, int kFilterWordsPerWarp>
 __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams prm, int exact) {
@@ -468,6 +477,54 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
     return word_here ? k * tiles + tile : tile * kFilterTileWords + k;
   };
   unsigned long long cand = 0, base = 0, bytes = 0, wchk = 0, wpass = 0;
+  if (word_here && NGIA_FILTER_WARP_WORD) {
+    // Short-word test here: the work per candidate grows with its length, so
+    // warps run independently — each takes every W-th bitmap word of the
+    // length-sorted database (a share of every length) and queues its
+    // survivors with one atomic per class and word; no CTA barrier makes a
+    // warp wait for the CTA's longest candidates.
+    const int W = gridDim.x * (blockDim.x >> 5);
+    for (int wi = blockIdx.x * (blockDim.x >> 5) + warp; wi < nbw; wi += W) {
+      const uint32_t bits = rb.alive[wi];
+      if (!bits) continue;  // warp-uniform
+      const int c = wi * 32 + lane;
+      const bool alive = (bits >> lane) & 1u;
+      bool pass = false, deferred = false;
+      int cls = 0;
+      if (alive) {
+        cand++;
+        bytes += 4 * (2 + A);
+        const int L2 = __ldg(db.len + c);
+        pass = !(base_sum<A>(db.cnt, c, s_rc) < cutoff_of(L2, s));
+        if (pass) {
+          base++;
+          const int net2 = __ldg(db.net + c);
+          wchk++;
+          bytes += 4ull * P * ((net2 + 31) / 32);
+          if (net2 <= kWarpWordLen) {
+            const uint32_t *planes = db.words + __ldg(db.off + c) + db.hw;
+            pass = !(word_count_fast<P>(planes, net2, prm.w, s_tab) < word_min(L2, prm.w, s));
+            if (pass) wpass++;
+          } else {
+            deferred = true;
+          }
+        }
+        if (pass) cls = class_of(db.type, window_of(band_blocks(L1, L2, s), nb1));
+      }
+      // long candidates go to k_filter_long, which gives each one a warp
+      const unsigned dm = __ballot_sync(kFullMask, deferred);
+      if (dm) {
+        const int leader = __ffs(dm) - 1;
+        uint32_t b = 0;
+        if (lane == leader) b = atomicAdd(&st->long_count, (uint32_t)__popc(dm));
+        b = __shfl_sync(kFullMask, b, leader);
+        if (deferred) rb.long_list[b + __popc(dm & ((1u << lane) - 1u))] = c;
+      }
+      push_queue(rb, st, pass && !deferred, cls, c);
+    }
+    flush_stats(rb, cand, base, bytes, wchk, wpass);
+    return;
+  }
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     if (threadIdx.x < kNumClasses) s_cnt[threadIdx.x] = 0;
     __syncthreads();
@@ -661,9 +718,55 @@ __global__ void __launch_bounds__(256) k_word_exact(DevDB db, RunBufs rb, RunPar
 }
 
 // Largest filter shared memory: DNA w=8 bitset (8 KB) + byte table (64 KB).
+// Short-word test of the candidates longer than kWarpWordLen residues that
+// k_filter queued in rb.long_list (word-first order): one warp per
+// candidate, spread over the grid, so that the longest sequences of the
+// length-sorted database (which share the first bitmap words) are counted
+// side by side; survivors join the alignment class queues.
+template <int P>
+__global__ void __launch_bounds__(256) k_filter_long(DevDB db, RunBufs rb, RunParams prm) {
+  RunState *st = rb.st;
+  extern __shared__ __align__(16) uint32_t s_list[];
+  __shared__ uint64_t bar;
+  __shared__ int s_hdr[4];
+  if (threadIdx.x == 0) {
+    const bool skip = st->done || st->iter >= st->iter_limit || st->err;
+    s_hdr[0] = skip ? 0 : (int)st->long_count;
+    s_hdr[1] = st->rep_len;
+    s_hdr[2] = st->rep_nb;
+  }
+  __syncthreads();
+  const int nlong = s_hdr[0];
+  if (nlong == 0) return;
+  const int L1 = s_hdr[1], nb1 = s_hdr[2];
+  const int list_words = max(1, (int)((1u << (prm.w * (P == 2 ? 2 : 5))) / 32u));
+  uint8_t *s_tab = reinterpret_cast<uint8_t *>(s_list + list_words);
+  if (!stage_to_smem(s_list, rb.rep_list, (uint32_t)list_words, &bar, st, 2)) return;
+  for (int i = threadIdx.x; i < list_words * 8; i += blockDim.x) {
+    const uint32_t nib = (s_list[i >> 3] >> (4 * (i & 7))) & 0xFu;
+    reinterpret_cast<uint32_t *>(s_tab)[i] = (nib & 1u) | ((nib & 2u) << 7) | ((nib & 4u) << 14) | ((nib & 8u) << 21);
+  }
+  __syncthreads();
+  const float s = prm.s;
+  const int lane = threadIdx.x & 31;
+  const int W = gridDim.x * (blockDim.x >> 5);
+  unsigned long long wpass = 0;
+  for (int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < nlong; k += W) {
+    const int c = rb.long_list[k];
+    const uint32_t *planes = db.words + __ldg(db.off + c) + db.hw;
+    const int ws = word_count_warp<P>(planes, __ldg(db.net + c), prm.w, s_tab);
+    const int L2 = __ldg(db.len + c);
+    const bool pass = lane == 0 && !(ws < word_min(L2, prm.w, s));
+    if (pass) wpass++;
+    push_queue(rb, st, pass, pass ? class_of(db.type, window_of(band_blocks(L1, L2, s), nb1)) : 0, c);
+  }
+  flush_stats(rb, 0, 0, 0, 0, wpass);
+}
+
 cudaError_t filter_configure() {
   const int most = 9 * (1 << 16) / 8;
-  const void *fns[] = {(const void *)k_filter<2, NGIA_FILTER_WPW_WORD>, (const void *)k_filter<5, NGIA_FILTER_WPW_WORD>};
+  const void *fns[] = {(const void *)k_filter<2, NGIA_FILTER_WPW_WORD>, (const void *)k_filter<5, NGIA_FILTER_WPW_WORD>,
+                       (const void *)k_filter_long<2>, (const void *)k_filter_long<5>};
   for (const void *f : fns) {
     cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
     if (e != cudaSuccess) return e;
@@ -690,6 +793,13 @@ cudaError_t launch_filter(ngia_ctx *c) {
         k_filter<2, kW><<<grid_w, 256, smem * 9, c->stream>>>(c->db, c->rb, c->prm, 0);
       else
         k_filter<5, kW><<<grid_w, 256, smem * 9, c->stream>>>(c->db, c->rb, c->prm, 0);
+      if (NGIA_FILTER_WARP_WORD && c->db.max_nb * 32 > kWarpWordLen) {  // some record is long
+        const int grid_l = std::max(1, std::min(c->grid_filter, c->num_sms));
+        if (P == 2)
+          k_filter_long<2><<<grid_l, 256, smem * 9, c->stream>>>(c->db, c->rb, c->prm);
+        else
+          k_filter_long<5><<<grid_l, 256, smem * 9, c->stream>>>(c->db, c->rb, c->prm);
+      }
     } else {
       if (P == 2)
         k_filter<2, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
