@@ -18,7 +18,7 @@ using ngia::fail;
 namespace {
 
 constexpr char kMagic[8] = {'N', 'G', 'I', 'A', 'C', 'K', 'P', '1'};
-constexpr uint32_t kVersion = 1;
+constexpr uint32_t kVersion = 2;  // 2: run state with the long-candidate count
 
 struct CkptHeader {
   char magic[8];
