@@ -288,12 +288,12 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       uint32_t cw = 0, ncw = 0;
       int base = js;
       for (int t = 0; t < full; t++, base += MT) {
-        zw += tiled_tile_eq<MT, NGIA_EQ_PF_MAIN, Ring>(ring, req, base, je, nb1, cols, q, cw, ncw);
+        zw += tiled_tile_eq<MT, NGIA_SERVE_PF, Ring>(ring, req, base, je, nb1, cols, q, cw, ncw);
         cw = ncw << (32 - cols);
         ncw = 0;
       }
       for (; rem >= MT; rem -= MT, base += MT) {
-        zw += tiled_tile_eq<MT, NGIA_EQ_PF_MAIN, Ring>(ring, req, base, je, nb1, cols, q, cw, ncw);
+        zw += tiled_tile_eq<MT, NGIA_SERVE_PF, Ring>(ring, req, base, je, nb1, cols, q, cw, ncw);
         cw = ncw << (32 - cols);
         ncw = 0;
       }

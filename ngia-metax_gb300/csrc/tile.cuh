@@ -43,6 +43,9 @@
 #ifndef NGIA_SERVE_EQ
 #define NGIA_SERVE_EQ 1
 #endif
+#ifndef NGIA_SERVE_PF
+#define NGIA_SERVE_PF 0
+#endif
 #ifndef NGIA_EQ_UNROLL
 #define NGIA_EQ_UNROLL 1
 #endif
