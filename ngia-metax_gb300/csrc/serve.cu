@@ -6,7 +6,9 @@
 //
 // Resident state (ngia_serve_open): the representatives as a device
 // database (records and header arrays, loaded by the same loader as
-// ngia_open) plus one k-mer bitset per representative, built on the device.
+// ngia_open) plus one k-mer bitset and, for DNA, one match table per
+// representative, built on the device.  The per-pair kernels are shared with
+// the speculative rounds (assign.cuh).
 //
 // One batch runs on one slot — a context of fixed capacity with its own
 // stream, driven by its own host thread:
@@ -23,7 +25,8 @@
 //     rounds stop once no query is left (or the set is exhausted);
 //  2. the leftovers are clustered by the greedy driver over the batch's
 //     database restricted to them (begin_subset), which equals clustering a
-//     database of only the leftovers.
+//     database of only the leftovers — by default with the speculative
+//     rounds (spec.cu).
 // Slots run side by side on the GPU; a batch waits in a FIFO until a slot is
 // free.  The number of slots is capped by the memory budget.
 #include <algorithm>
