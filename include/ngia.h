@@ -139,7 +139,8 @@ typedef struct ngia_ctx ngia_ctx;
 #define NGIA_MODE_GRAPH  1  /* device-side driver in a captured CUDA graph
                                (conditional while node), no host round trip  */
 #define NGIA_MODE_SPEC   2  /* speculative rounds once the unclustered set is
-                               small (<= 262,144 sequences): the next K of them
+                               small (<= 524,288 sequences: K >= 2 candidates
+                               with K x unclustered <= 2^20 pairs): the next K
                                are candidate representatives of one round,
                                every pair against them runs at once and the
                                greedy order is replayed on the device (same

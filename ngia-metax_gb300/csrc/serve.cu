@@ -357,8 +357,8 @@ int64_t slot_bytes(const ngia_server *sv, int grid2) {
   const int64_t rounds = (int64_t)kServeClasses * kMaxChunk * sv->cap_n * 8 + sv->cap_n * 8 + sv->cap_n / 8;
   const int64_t scratch = (int64_t)grid2 * kAlignThreads * (sv->ring_mask + 1) * 4;
   // speculative leftover rounds: masks, up to 64 scores per record, pair
-  // queues of 2^18 pairs per class, their own global ring
-  const int64_t spec = sv->cap_n * (8 + 64 * 4) + (int64_t)kServeClasses * (1 << 18) * 8 + scratch;
+  // queues of 2^20 pairs per class, their own global ring
+  const int64_t spec = sv->cap_n * (8 + 64 * 4) + (int64_t)kServeClasses * (1 << 20) * 8 + scratch;
   return ctx + rounds + scratch + spec + (16 << 20);
 }
 

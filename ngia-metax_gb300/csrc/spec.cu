@@ -44,7 +44,7 @@ namespace ngia {
 namespace {
 
 constexpr int kSpecMax = 64;              // candidate representatives per round (one mask bit each)
-constexpr int kSpecBudget = 1 << 18;      // pairs per round at most (K x unclustered)
+constexpr int kSpecBudget = 1 << 20;      // pairs per round at most (K x unclustered)
 constexpr int64_t kSpecScoreWords = 1ll << 26;  // K x n scores at most (256 MB)
 
 struct SpecCtl {
@@ -95,8 +95,10 @@ __global__ void __launch_bounds__(1024) k_spec_pick(DevDB db, RunBufs run, SpecD
   if (tid == 0) {
     int k = 0;
     const int64_t rem = st->iter_limit - st->iter;
-    if (total > 0 && total <= budget && !st->err && rem > 0) {
-      k = min(k_max, max(1, budget / total));
+    // at least two candidates per round (one is a plain iteration, which
+    // the clustering kernels run faster)
+    if (total > 0 && (int64_t)total * 2 <= budget && k_max >= 2 && !st->err && rem > 0) {
+      k = min(k_max, budget / total);
       k = min(k, total);
       if (rem < k) k = (int)rem;
     }
