@@ -194,7 +194,7 @@ def params_clamp(db_type: int, similarity: float, word_length: int, precise: int
     return p
 
 
-# ---- synthetic workloads (the five BASELINE configurations) -----------------
+# ---- synthetic workloads (the five benchmark configurations) ----------------
 CONFIGS = {
     # 20,000 DNA from 400 ancestors, N(1450, 80) clipped [1200, 1700]
     "dna_small": dict(type=0, len_dist=0, n_seqs=20000, n_ancestors=400, len_a=1450.0, len_b=80.0,

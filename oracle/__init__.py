@@ -1,2 +1,3 @@
 """CPU oracle of the reference clustering — test infrastructure only (the
-parity checker and the CPU baseline); the product never imports it."""
+reference results the parity tests compare against, and the CPU baseline);
+the product never imports it."""

@@ -1,9 +1,9 @@
 /*
  * ngia_oracle.c — line-faithful CPU restatement of nGIA's single-node
  * clustering, CUDA/signalNode/src/func.cu (same algorithm in
- * OneAPI/SignalNode/src/func.cpp).  TEST INFRASTRUCTURE: it is the parity
- * checker and the timed CPU baseline; the product library never links,
- * loads or calls it.
+ * OneAPI/SignalNode/src/func.cpp).  TEST INFRASTRUCTURE: it gives the
+ * results the parity tests compare against and the timed CPU baseline; the
+ * product library never links, loads or calls it.
  *
  * Parity pins: the database format is pinned against the reference makeDB
  * tool built from its own sources (oracle/build_ref.sh); the clustering

@@ -1,8 +1,8 @@
 /*
  * ngia_oracle.h — CPU restatement of nGIA's single-node clustering
- * (CUDA/signalNode/src/func.cu) used as the parity checker and the timed CPU
- * baseline.  TEST INFRASTRUCTURE ONLY: the product library never links,
- * loads or calls it.
+ * (CUDA/signalNode/src/func.cu) used as the parity reference of the tests
+ * and the timed CPU baseline.  TEST INFRASTRUCTURE ONLY: the product library
+ * never links, loads or calls it.
  */
 #ifndef NGIA_ORACLE_H
 #define NGIA_ORACLE_H

@@ -1,7 +1,8 @@
 """ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, the smoke check and the CPU
-baseline leg of bench.py as the checker; the product never imports it.
+baseline leg of bench.py as the reference results; the product never
+imports it.
 """
 from __future__ import annotations
 
