@@ -234,6 +234,11 @@ def run_ours(args, dist: Dist):
 
     ctx = ngia.Context(db)
     tuning = ctx.autotune(p, args.autotune) if args.autotune > 0 else None  # before the timed region
+    # short words first with records over 2,048 residues: k_filter_long too
+    wo = tuning["word_order"] if tuning else 0
+    word_first = wo == 1 or (wo == 0 and (cfg["type"] == 1 or p.similarity >= 0.93))
+    if word_first and not p.precise and int(db.words[db.rec_off + 1].max()) > 2048:
+        launches_per_iter += 1
     ctx.begin(p, mode)
     for _ in range(args.warmup):
         ctx.step(S)
