@@ -147,10 +147,10 @@ typedef struct ngia_ctx ngia_ctx;
                                result as the one-representative loop); host
                                loop per round.  Plain iterations while the
                                set is larger, and throughout when the database
-                               has records of net length < 16 and precise is
-                               0 (the reference's short-word kernel then makes
-                               a pair's test depend on its iteration's job
-                               list).                                        */
+                               has records of net length < 16, precise is 0
+                               and more than 16,384 sequences (the reference's
+                               short-word kernel then makes a pair's test
+                               depend on its iteration's job list).          */
 
 typedef struct ngia_stats {
     int64_t iterations;    /* representatives taken (= clusters)             */

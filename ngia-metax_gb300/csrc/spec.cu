@@ -22,8 +22,9 @@
 // per-pair tests are pure functions of the pair, except the reference's
 // short-word kernel, whose thread leaves at its first job of net length < 16
 // (the job list of one iteration decides which later pairs skip the test):
-// with such records and the short-word test on (precise off), the driver
-// runs the plain loop instead.  K is sized so that a round's pairs stay within
+// with such records, the short-word test on (precise off) and more sequences
+// than the reference's 16,384 threads, the driver runs the plain loop
+// instead.  K is sized so that a round's pairs stay within
 // a budget (a few waves of the alignment kernels); while the unclustered set
 // is larger than that budget the plain one-representative iteration runs.
 #include <algorithm>
@@ -448,7 +449,12 @@ int spec_read(ngia_ctx *c) {
 
 }  // namespace
 
-bool spec_exact(const ngia_ctx *c) { return !c->db.has_short || c->prm.precise; }
+// With at most kRefGridThreads sequences every thread of the reference's
+// short-word kernel holds at most one job, so its early return only leaves
+// the short job itself untested — the pairwise rule of the round kernels.
+bool spec_exact(const ngia_ctx *c) {
+  return !c->db.has_short || c->prm.precise || c->db.n <= kRefGridThreads;
+}
 
 int spec_prepare(ngia_ctx *c) {
   int rc = spec_alloc(c);

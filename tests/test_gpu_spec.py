@@ -60,9 +60,11 @@ def test_spec_long_records_word_first(cuda_device, db_type, s, w):
 
 @pytest.mark.parametrize("precise", [0, 1])
 def test_spec_short_records(cuda_device, precise):
-    """Records of net length < 16: with the short-word test on, a pair's test
-    depends on its iteration's job list, so the driver runs the plain loop;
-    in precise mode the rounds run."""
+    """Records of net length < 16 skip the short-word test.  Up to 16,384
+    sequences (one job per thread of the reference's word kernel) that is a
+    rule of the pair and the rounds run; beyond, a pair's test depends on its
+    iteration's job list and the driver runs the plain loop (precise mode:
+    no short-word test, rounds at any size)."""
     db = noisy_db(0, 500, seed=12, short_records=25)
     assert (db.words[db.rec_off + 1] < 16).any()
     _check_spec(db, ngia.params_clamp(0, 0.88, 7, precise))

@@ -392,11 +392,15 @@ def _replay_rounds(db, p, k):
     return cl, idn, reps
 
 
-@pytest.mark.parametrize("db_type,s,w,k", [(0, 0.85, 5, 4), (0, 0.85, 5, 64), (0, 0.95, 5, 16), (1, 0.5, 2, 64)])
-def test_speculative_rounds_replay_the_greedy_loop(db_type, s, w, k):
+@pytest.mark.parametrize("db_type,s,w,k,short", [(0, 0.85, 5, 4, 0), (0, 0.85, 5, 64, 0), (0, 0.95, 5, 16, 0),
+                                                  (1, 0.5, 2, 64, 0), (0, 0.88, 7, 8, 1)])
+def test_speculative_rounds_replay_the_greedy_loop(db_type, s, w, k, short):
     """The round resolution of the spec driver (csrc/spec.cu) gives the
-    greedy loop's clustering exactly, whatever the round size."""
-    db = family_db(db_type, n=120, anc=5, seed=3 + db_type)
+    greedy loop's clustering exactly, whatever the round size — also with
+    records of net length < 16, which skip the short-word test, when there are
+    at most 16,384 sequences (one job per thread of the reference kernel)."""
+    db = noisy_db(0, 200, seed=12, short_records=20) if short else family_db(db_type, n=120, anc=5,
+                                                                                seed=3 + db_type)
     p = ngia.params_clamp(db_type, s, w, 0)
     ocl, oid, ost = oracle.cluster(db.words, db.rec_off, db_type, p.similarity, p.word_length, p.precise)
     cl, idn, reps = _replay_rounds(db, p, k)
