@@ -36,6 +36,35 @@ def test_device_count_without_gpu_is_not_an_error():
     assert ngia.device_count() >= 0
 
 
+def test_entry_points_reject_null_arguments():
+    """Every stateful entry point checks its arguments before any device
+    work and returns NGIA_E_ARG (-1) with a message; no GPU is needed."""
+    import ctypes as C
+
+    L = ngia.lib()
+    prm = ngia.Params(0.9, 5, 0)
+    out = C.c_void_p()
+    assert L.ngia_cluster_begin(None, C.byref(prm), ngia.MODE_SPEC) == -1
+    assert L.ngia_cluster_step(None, 1, None) == -1
+    assert L.ngia_cluster_save(None, b"x") == -1
+    assert L.ngia_cluster_resume(None, b"x", ngia.MODE_GRAPH) == -1
+    assert L.ngia_reload(None, None) == -1
+    assert L.ngia_autotune(None, C.byref(prm), 4, None) == -1
+    assert L.ngia_set_tuning(None, None) == -1
+    assert L.ngia_batch_open(None, 0, C.byref(out)) == -1
+    assert L.ngia_serve_open(None, C.byref(prm), None, C.byref(out)) == -1
+    assert L.ngia_serve_submit(None, None, None) == -1
+    assert L.ngia_serve_poll(None, 1, 0, None, None, None) == -1
+    assert L.ngia_params_clamp(2, C.byref(prm)) == -1
+    buf = C.create_string_buffer(256)
+    L.ngia_last_error(buf, 256)
+    assert b"type 2" in buf.value
+    # the driver-form constants of the header and the binding agree
+    hdr = (ROOT / "include" / "ngia.h").read_text()
+    for name, val in (("PLAIN", ngia.MODE_PLAIN), ("GRAPH", ngia.MODE_GRAPH), ("SPEC", ngia.MODE_SPEC)):
+        assert re.search(rf"#define NGIA_MODE_{name}\s+{val}\b", hdr), name
+
+
 @pytest.mark.parametrize("db_type", [0, 1])
 def test_params_clamp_matches_oracle(db_type):
     for s in np.concatenate([np.linspace(0.0, 1.2, 61), [0.75, 0.81, 0.84, 0.86, 0.88, 0.5, 0.7, 0.7499999]]):
