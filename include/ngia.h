@@ -167,6 +167,8 @@ typedef struct ngia_stats {
     double  ms_align;      /* of the alignment launches (profiling, plain)   */
     int64_t class_pairs[8];   /* pairs queued per alignment work class       */
     double  class_ms[8];      /* device time per class (profiling, plain)    */
+    int64_t class_cells[8];   /* in-band cells computed per class            */
+    int64_t class_bytes[8];   /* query plane bytes of the pairs per class    */
 } ngia_stats;
 
 /* Copies the database to the device (one host-to-device transfer) and
@@ -332,9 +334,13 @@ int ngia_measure_int_peak(double *gops);
  * of this library (held by every GPU that loads it until the process exits),
  * which limits the representative to 65,536 residues (NGIA_E_LIMIT beyond).
  * The first call on a device looks the array up and must precede any stream
- * capture; calls that overlap on the GPU share the array and race — serialise
- * them.  Work is queued on `stream` (NULL = default stream); the scores are
- * ready when it completes. */
+ * capture; the address is kept for the life of the process, so do not call
+ * this across a cudaDeviceReset of that device.  Calls that overlap on the
+ * GPU share the array and race — serialise them.  Each call first reads the
+ * representative's two header words back to the host (to size its grid), so
+ * it waits until `stream` (NULL = default stream) has reached that point;
+ * the kernel is then queued on `stream` and the scores are ready when it
+ * completes. */
 int ngia_rep_scores_noalloc(const uint32_t *d_words, int64_t rep_off,
                             const int64_t *d_query_off, int32_t n, int32_t type,
                             float similarity, int32_t *d_scores, void *stream);

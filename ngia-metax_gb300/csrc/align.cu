@@ -104,10 +104,10 @@ __device__ __forceinline__ bool align_setup(const DevDB &db, const RunBufs &rb, 
     }
   }
   __syncthreads();
-  bool ok = mbar_wait_bounded(bar, 0, 1u << 20);
+  bool ok = mbar_wait_bounded(bar, 0, prm.wait_polls);
   if (!ok) {
     set_error(st, NGIA_ERR_MBAR_TIMEOUT, 10 + cls);
-    mbar_wait_bounded(bar, 0, 1u << 20);
+    mbar_wait_bounded(bar, 0, kWaitPolls);  // let the copy in flight land
   }
   return __syncthreads_and(ok);
 }
@@ -170,9 +170,9 @@ __device__ __forceinline__ void finish_pair(const DevDB &db, const RunBufs &rb, 
   }
 }
 
-__device__ __forceinline__ void flush_align_stats(RunState *st, unsigned long long pairs,
+__device__ __forceinline__ void flush_align_stats(RunState *st, int cls, unsigned long long pairs,
                                                   unsigned long long members, unsigned long long cells,
-                                                  unsigned long long done) {
+                                                  unsigned long long done, unsigned long long *s_qwords) {
   for (int o = 16; o; o >>= 1) {
     pairs += __shfl_down_sync(kFullMask, pairs, o);
     members += __shfl_down_sync(kFullMask, members, o);
@@ -183,8 +183,13 @@ __device__ __forceinline__ void flush_align_stats(RunState *st, unsigned long lo
     if (pairs) atomicAdd(&st->st_align_pairs, pairs);
     if (members) atomicAdd(&st->st_members, members);
     if (cells) atomicAdd(&st->st_band_cells, cells);
-    if (done) atomicAdd(&st->st_done_cells, done * 32ull);
+    if (done) {
+      atomicAdd(&st->st_done_cells, done * 32ull);
+      atomicAdd(&st->st_class_done[cls], done * 32ull);
+    }
   }
+  __syncthreads();
+  if (threadIdx.x == 0 && *s_qwords) atomicAdd(&st->st_class_qwords[cls], *s_qwords);
 }
 
 template <int P, int WC>
@@ -193,6 +198,8 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
   AlignHdr h;
+  __shared__ unsigned long long s_qw;  // query plane words of the pairs taken (algorithmic bytes / 4)
+  if (threadIdx.x == 0) s_qw = 0;
   if (!align_setup<P>(db, rb, prm, cls, score_mode, warp_pairs, 0, smem, &bar, h)) return;
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
@@ -236,6 +243,7 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
       if (!score_mode) {
         n_pairs++;
         n_cells += (unsigned long long)band_cells(B, nb1, net2);
+        atomicAdd(&s_qw, (unsigned long long)(nq * P));
       }
       if (B < 0 || je < 0 || nq == 0) {
         finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, 0, cutoff, L2, net2, qpl, s_list, n_members);
@@ -355,7 +363,7 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
 #pragma unroll
     for (int p = 0; p < P; p++) cur[p] = nxt[p];
   }
-  flush_align_stats(st, n_pairs, n_members, n_cells, n_done);
+  flush_align_stats(st, cls, n_pairs, n_members, n_cells, n_done, &s_qw);
 }
 
 
@@ -382,6 +390,8 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
   AlignHdr h;
+  __shared__ unsigned long long s_qw;  // query plane words of the pairs taken (algorithmic bytes / 4)
+  if (threadIdx.x == 0) s_qw = 0;
   if (!align_setup<P>(db, rb, prm, cls, score_mode, warp_pairs, 0, smem, &bar, h)) return;
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
@@ -447,6 +457,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       if (!score_mode) {
         n_pairs++;
         n_cells += (unsigned long long)band_cells(B, nb1, net2);
+        atomicAdd(&s_qw, (unsigned long long)(nq * P));
       }
       if (B < 0 || je < 0 || nq == 0) {
         finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, 0, cutoff, L2, net2, qpl, s_list, n_members);
@@ -539,7 +550,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 #pragma unroll
     for (int p = 0; p < P; p++) cur[p] = nxt[p];
   }
-  flush_align_stats(st, n_pairs, n_members, n_cells, n_done);
+  flush_align_stats(st, cls, n_pairs, n_members, n_cells, n_done, &s_qw);
 }
 
 
@@ -694,6 +705,8 @@ __global__ void __launch_bounds__(kAlignThreads)
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint64_t bar;
   AlignHdr h;
+  __shared__ unsigned long long s_qw;  // query plane words of the pairs taken (algorithmic bytes / 4)
+  if (threadIdx.x == 0) s_qw = 0;
   if (!align_setup<P>(db, rb, prm, cls, score_mode, warp_pairs, 1, smem, &bar, h)) return;
   const uint32_t *s_pl = smem;
   const uint32_t *s_list = smem + ((h.nb1 * P + 3) & ~3);
@@ -717,6 +730,7 @@ __global__ void __launch_bounds__(kAlignThreads)
     if (!score_mode && lane == 0) {
       n_pairs++;
       n_cells += (unsigned long long)band_cells(B, nb1, net2);
+      atomicAdd(&s_qw, (unsigned long long)(nq * P));
     }
     if (B < 0 || nq == 0) {
       if (lane == 0) finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, 0, cutoff, L2, net2, qpl, s_list, n_members);
@@ -735,7 +749,7 @@ __global__ void __launch_bounds__(kAlignThreads)
     if (lane == 0) finish_pair<P>(db, rb, prm, h, score_mode, entry, cand, sum, cutoff, L2, net2, qpl, s_list, n_members);
     __syncwarp();
   }
-  flush_align_stats(st, n_pairs, n_members, n_cells, n_done);
+  flush_align_stats(st, cls, n_pairs, n_members, n_cells, n_done, &s_qw);
 }
 
 // ---- dispatch ---------------------------------------------------------------------

@@ -111,6 +111,8 @@ void fill_stats(const ngia_ctx *c, ngia_stats *stats) {
   for (int k = 0; k < 8; k++) {
     stats->class_pairs[k] = k < ngia::kNumClasses ? (int64_t)s.st_class_pairs[k] : 0;
     stats->class_ms[k] = k < ngia::kNumClasses ? c->ms_class[k] : 0.0;
+    stats->class_cells[k] = k < ngia::kNumClasses ? (int64_t)s.st_class_done[k] : 0;
+    stats->class_bytes[k] = k < ngia::kNumClasses ? 4 * (int64_t)s.st_class_qwords[k] : 0;
   }
 }
 
@@ -158,7 +160,8 @@ int build_graph(ngia_ctx *c) {
 }
 
 bool same_params(const ngia::RunParams &a, const ngia::RunParams &b) {
-  return a.s == b.s && a.w == b.w && a.precise == b.precise && a.word_order == b.word_order && a.refill == b.refill;
+  return a.s == b.s && a.w == b.w && a.precise == b.precise && a.word_order == b.word_order && a.refill == b.refill &&
+         a.wait_polls == b.wait_polls;
 }
 
 int validate_params(int type, const ngia_params *p) {
@@ -485,10 +488,17 @@ int ngia::drv::begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, con
   if (const char *rf = getenv("NGIA_REFILL")) c->prm.refill = std::max(1, std::min(32, atoi(rf)));
   if (!getenv("NGIA_WARP_PAIRS")) c->warp_pairs = c->tuned_warp_pairs >= 0 ? c->tuned_warp_pairs : c->warp_pairs_default;
   if (c->db.has_short && !c->prm.precise) c->prm.word_order = 1;  // exact path is word first
+  // NGIA_WAIT_POLLS lowers the poll limit of the alignment kernels' staging
+  // wait; at 0 every such wait gives up at once, which is how the tests make
+  // the device-side error path (NGIA_E_DEVICE, context still usable) run
+  c->prm.wait_polls = ngia::kWaitPolls;
+  if (const char *wp = getenv("NGIA_WAIT_POLLS"))
+    c->prm.wait_polls = (uint32_t)std::max<long long>(0, std::min<long long>(atoll(wp), ngia::kWaitPolls));
   c->mode = mode;
   c->ms_filter = c->ms_align = 0.0;
   for (double &m : c->ms_class) m = 0.0;
   c->last_step_ms = 0.f;
+  c->begun = false;  // no steppable run until the new one is fully set up
   CK(ngia::launch_init_run(c));
   if (d_alive) CK(ngia::launch_subset_start(c, d_alive));
   rc = pull_state(c);
@@ -626,6 +636,7 @@ extern "C" int ngia_pair_scores(ngia_ctx *c, const ngia_params *p, int32_t rep, 
   c->prm.w = p->word_length;
   c->prm.precise = p->precise;
   c->prm.refill = 32;
+  c->prm.wait_polls = ngia::kWaitPolls;
   int32_t *d_c = nullptr, *d_o = nullptr;
   CK(dalloc(&d_c, (size_t)n));
   CK(dalloc(&d_o, 4 * (size_t)n));

@@ -162,6 +162,13 @@ extern "C" int ngia_cluster_resume(ngia_ctx *c, const char *path, int32_t mode) 
   const ngia_params p = {h.similarity, h.word_length, h.precise};
   rc = ngia::drv::validate_params(c->db.type, &p);
   if (rc) return rc;
+  // the same ranges ngia_set_tuning accepts: the checksum only catches
+  // accidental damage, not a well-formed file with settings out of range
+  if (h.word_order < 0 || h.word_order > 2 || h.refill < 1 || h.refill > 32)
+    return fail(NGIA_E_FORMAT, "ngia_cluster_resume: %s holds tuning settings out of range", path);
+  // from the first device write on, the context holds no run that can be
+  // stepped until the driver of the resumed run is ready
+  c->begun = false;
   c->prm.s = h.similarity;
   c->prm.w = h.word_length;
   c->prm.precise = h.precise;

@@ -77,7 +77,13 @@ struct RunState {
   unsigned long long st_band_cells, st_filter_bytes, st_word_checks, st_word_pass;
   unsigned long long st_done_cells;  // in-band cells actually computed
   unsigned long long st_class_pairs[kNumClasses];
+  unsigned long long st_class_done[kNumClasses];    // in-band cells computed per class
+  unsigned long long st_class_qwords[kNumClasses];  // query plane words of the pairs per class
 };
+
+// Polls of an mbarrier wait before a kernel gives up (each poll blocks for a
+// hardware-defined interval; a staging copy lands within a few polls).
+constexpr uint32_t kWaitPolls = 1u << 20;
 
 // Run parameters (constant during one clustering).
 struct RunParams {
@@ -86,6 +92,7 @@ struct RunParams {
   int32_t precise;
   int32_t word_order;     // 0 auto, 1 word first, 2 alignment first
   int32_t refill;         // tiled alignment: idle lanes a warp waits for before it claims new pairs
+  uint32_t wait_polls = kWaitPolls;  // poll limit of the alignment kernels' staging wait
 };
 
 // Order of the two cheap-to-expensive tests.  Both orders give the same

@@ -88,7 +88,7 @@ __global__ void k_init_run(DevDB db, RunBufs rb, RunParams prm) {
     st->st_band_cells = st->st_filter_bytes = st->st_word_checks = st->st_word_pass = 0;
     st->st_done_cells = 0;
     for (int k = 0; k < kFilterStripes * kFilterStats; k++) rb.fstats[k] = 0;
-    for (int k = 0; k < kNumClasses; k++) st->st_class_pairs[k] = 0;
+    for (int k = 0; k < kNumClasses; k++) st->st_class_pairs[k] = st->st_class_done[k] = st->st_class_qwords[k] = 0;
   }
 }
 

@@ -18,10 +18,14 @@
 // Host code must not use the array's name as a device address: the first call
 // on each device looks its address up with cudaGetSymbolAddress (with that
 // device current) and caches it; make that first call before any stream
-// capture.  All calls share the array, so calls whose kernels overlap on the
-// GPU (different streams, or concurrent host threads) race on it; serialise
-// them.  Nothing in the array has to start at zero: each thread initialises
-// its row for every pair it scores.
+// capture.  The cached address belongs to the module loaded in the device's
+// primary context: after a cudaDeviceReset it would be stale, so the entry
+// point is not for use across a device reset.  Each call copies the
+// representative's two header words to the host to size its grid, which
+// waits for `stream` to reach that copy.  All calls share the array, so calls
+// whose kernels overlap on the GPU (different streams, or concurrent host
+// threads) race on it; serialise them.  Nothing in the array has to start at
+// zero: each thread initialises its row for every pair it scores.
 #include <cuda_runtime.h>
 
 #include <algorithm>

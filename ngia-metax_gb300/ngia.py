@@ -67,7 +67,8 @@ class Stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("iterations", "candidates", "base_pass", "align_pairs", "members",
                                          "band_cells", "filter_bytes", "word_checks", "done_cells")] + \
         [("ms_filter", C.c_double), ("ms_align", C.c_double), ("class_pairs", C.c_int64 * 8),
-         ("class_ms", C.c_double * 8)]
+         ("class_ms", C.c_double * 8), ("class_cells", C.c_int64 * 8),
+         ("class_bytes", C.c_int64 * 8)]
 
     def as_dict(self) -> dict:
         d = {}

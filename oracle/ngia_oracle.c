@@ -6,10 +6,13 @@
  * product library never links, loads or calls it.
  *
  * Parity pins: the database format is pinned against the reference makeDB
- * tool built from its own sources (oracle/build_ref.sh); the clustering
- * arithmetic is pinned by the known-answer cases in tests/golden (exact LCS
- * when the band covers the matrix, the fused-multiply-add band case) and by
- * the reference's own CUDA build where it can run on a GPU.
+ * tool built from its own source (oracle/build_oracle.py); the clustering is
+ * pinned by the reference's own CUDA program, built from its sources and run
+ * on a GB300 (oracle/ref_cluster.py), whose outputs for 4 fixtures x 15
+ * parameter sets are committed under tests/golden/ref/ and reproduced byte
+ * for byte (tests/test_host_cpu.py::test_oracle_matches_reference_golden),
+ * and by known-answer cases in tests/test_host_cpu.py (exact LCS when the
+ * band covers the matrix, the fused-multiply-add band case).
  *
  * Compiled with -ffp-contract=off: the only fused multiply-add is the
  * explicit fmaf() of the band shift, which nvcc contracts in the reference

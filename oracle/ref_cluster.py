@@ -2,7 +2,7 @@
 produce golden outputs.  Test infrastructure.
 
     python oracle/ref_cluster.py stage        # where the reference tree exists
-    python oracle/ref_cluster.py run OUTDIR   # on a GPU host
+    python oracle/ref_cluster.py run OUTDIR [FIXTURE ...]   # on a GPU host
 
 `stage` copies the program's five source files (cluster.cpp, func.cu,
 func.h, cmdline.h, timer.h) unchanged into baseline/_ref/signalNode/ — the
@@ -16,7 +16,12 @@ Makefile line does (nvcc src/cluster.cpp src/func.cu -o cluster), adding only
 database with the makeDB drop-in (byte-identical to the reference makeDB, see
 manifest.json), runs the reference on every parameter set twice, and copies
 cluster.txt / represent.fasta to OUTDIR/<fixture>/<tag>/ (flagging any run
-whose two outputs differ).
+whose two outputs differ).  For a generated fixture (manifest "generated")
+the FASTA is written from its generator first and the outputs are recorded
+as md5s in OUTDIR/<fixture>/<tag>/outputs.json.
+
+The reference tree is read where this build container mounts it
+(NGIA_REFERENCE_DIR overrides the location); only `stage` reads it.
 """
 from __future__ import annotations
 
@@ -53,9 +58,17 @@ def build() -> Path:
     return exe
 
 
-def run(outdir: str) -> None:
+def _md5(path: Path) -> str:
+    import hashlib
+
+    return hashlib.md5(path.read_bytes()).hexdigest()
+
+
+def run(outdir: str, only: list[str] | None = None) -> None:
     sys.path.insert(0, str(ROOT / "ngia-metax_gb300"))
+    sys.path.insert(0, str(ROOT))
     import ngia
+    from tests.golden.make_golden import fixture_fasta
 
     exe = build()
     golden = ROOT / "tests" / "golden"
@@ -63,9 +76,11 @@ def run(outdir: str) -> None:
     out = Path(outdir)
     report = {}
     for name, m in manifest.items():
+        if only and name not in only:
+            continue
         dbdir = out / "_db" / name
         dbdir.mkdir(parents=True, exist_ok=True)
-        shutil.copyfile(golden / f"{name}.fasta", dbdir / "in.fasta")
+        shutil.copyfile(fixture_fasta(name, m, dbdir), dbdir / "in.fasta")
         ngia.makedb(str(dbdir / "in.fasta"), str(dbdir), m["type"])
         for s, w, p in m["params"]:
             tag = f"s{s}_w{w}_p{p}"
@@ -80,8 +95,17 @@ def run(outdir: str) -> None:
                              (od / "cluster.txt").exists() else b""))
             same = runs[0][2] == runs[1][2]
             final = out / name / tag
-            for f in ("cluster.txt", "represent.fasta"):
-                shutil.copyfile(final / "run0" / f, final / f)
+            if m.get("generated"):
+                n_clusters = sum(1 for ln in (final / "run0" / "cluster.txt").read_bytes().splitlines()
+                                 if not ln.startswith(b" "))
+                (final / "outputs.json").write_text(json.dumps(
+                    {f: _md5(final / "run0" / f) for f in ("cluster.txt", "represent.fasta")} |
+                    {"clusters": n_clusters}, indent=1) + "\n")
+            else:
+                for f in ("cluster.txt", "represent.fasta"):
+                    shutil.copyfile(final / "run0" / f, final / f)
+            for k in range(2):
+                shutil.rmtree(final / f"run{k}", ignore_errors=True)
             report[f"{name}/{tag}"] = {"rc": [r[0] for r in runs], "seconds": [round(r[1], 3) for r in runs],
                                        "deterministic": same}
     (out / "report.json").write_text(json.dumps(report, indent=1) + "\n")
@@ -133,7 +157,7 @@ if __name__ == "__main__":
     if sys.argv[1] == "stage":
         stage()
     elif sys.argv[1] == "run":
-        run(sys.argv[2])
+        run(sys.argv[2], sys.argv[3:] or None)
     elif sys.argv[1] == "compare":
         import argparse
 

@@ -11,6 +11,11 @@ The reference's clustering program only runs on a GPU; its outputs for every
 oracle/ref_cluster.py and committed under tests/golden/ref/<fixture>/<tag>/
 (cluster.txt, represent.fasta).  `python tests/golden/make_golden.py check`
 re-verifies the checksums.
+
+Fixtures of kind "q1" (tests/golden/q1_fixture.py) are too large to commit
+as FASTA; their bytes come from a seeded generator and the manifest pins
+their md5 (`fasta_md5`) beside the data.bin md5.  For them the reference's
+outputs are committed as md5s (tests/golden/ref/<fixture>/<tag>/outputs.json).
 """
 from __future__ import annotations
 
@@ -26,8 +31,10 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
 sys.path.insert(0, str(ROOT / "ngia-metax_gb300"))
+sys.path.insert(0, str(ROOT))
 
 import ngia  # noqa: E402
+from tests.golden import q1_fixture  # noqa: E402
 
 # (name, type, generator args, edits, parameter sets [s, w, p])
 FIXTURES = [
@@ -40,7 +47,20 @@ FIXTURES = [
     ("prot_a", 1, dict(type=1, len_dist=1, n_seqs=240, n_ancestors=8, len_a=180.0, len_b=0.6, len_min=20,
                        len_max=1200, subst_max=0.5, indel_max=5, seed=303),
      "plain", [(0.9, 3, 0), (0.5, 2, 0), (0.7, 3, 0), (0.45, 3, 0)]),
+    ("dna_q1", 0, None, "q1", q1_fixture.PARAMS),
 ]
+
+
+def fixture_fasta(name: str, m: dict, workdir: Path) -> Path:
+    """Path of a fixture's FASTA: the committed file, or for a generated
+    fixture a fresh copy written into workdir and checked against its md5."""
+    if m.get("generated") != "q1":
+        return HERE / f"{name}.fasta"
+    fa = Path(workdir) / f"{name}.fasta"
+    facts = q1_fixture.write(fa)
+    if facts["fasta_md5"] != m["fasta_md5"]:
+        raise RuntimeError(f"{name}: generated FASTA md5 {facts['fasta_md5']} != manifest {m['fasta_md5']}")
+    return fa
 
 
 def _noisy(seqs: list[bytes], seed: int) -> list[bytes]:
@@ -80,24 +100,34 @@ def tag(s: float, w: int, p: int) -> str:
     return f"s{s}_w{w}_p{p}"
 
 
-def make_fasta() -> None:
+def make_fasta(only: list[str] | None = None) -> None:
     ref_makedb = ROOT / "oracle" / "_ref" / "makeDB"
     if not ref_makedb.exists():
         raise SystemExit("oracle/_ref/makeDB missing: run oracle/build_oracle.py where the reference tree exists")
-    manifest = {}
+    path = HERE / "manifest.json"
+    manifest = json.loads(path.read_text()) if only and path.exists() else {}
     for name, typ, gen, kind, params in FIXTURES:
-        seq, off = ngia.synth(**gen)
-        seqs = seq.all_bytes()
-        if kind == "noisy":
-            seqs = _noisy(seqs, gen["seed"])
-        fa = HERE / f"{name}.fasta"
-        _write_fasta(fa, seqs, crlf_every=5 if kind == "noisy" else 0)
+        if only and name not in only:
+            continue
         with tempfile.TemporaryDirectory() as td:
-            subprocess.run([str(ref_makedb), "-i", str(fa), "-o", td, "-t", str(typ)], check=True,
+            extra = {}
+            if kind == "q1":
+                fa = Path(td) / f"{name}.fasta"
+                extra = {"generated": "q1", "fasta_md5": q1_fixture.write(fa)["fasta_md5"]}
+            else:
+                seq, off = ngia.synth(**gen)
+                seqs = seq.all_bytes()
+                if kind == "noisy":
+                    seqs = _noisy(seqs, gen["seed"])
+                fa = HERE / f"{name}.fasta"
+                _write_fasta(fa, seqs, crlf_every=5 if kind == "noisy" else 0)
+            out = Path(td) / "db"
+            out.mkdir()
+            subprocess.run([str(ref_makedb), "-i", str(fa), "-o", str(out), "-t", str(typ)], check=True,
                            capture_output=True)
-            manifest[name] = {"type": typ, "data_bin_md5": md5(Path(td) / "data.bin"),
+            manifest[name] = {"type": typ, **extra, "data_bin_md5": md5(out / "data.bin"),
                               "params": [list(p) for p in params]}
-    (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1) + "\n")
+    path.write_text(json.dumps(manifest, indent=1) + "\n")
     print("wrote", ", ".join(manifest))
 
 
@@ -105,10 +135,14 @@ def check() -> None:
     manifest = json.loads((HERE / "manifest.json").read_text())
     for name, m in manifest.items():
         with tempfile.TemporaryDirectory() as td:
-            ngia.makedb(str(HERE / f"{name}.fasta"), td, m["type"])
+            ngia.makedb(str(fixture_fasta(name, m, Path(td))), td, m["type"])
             assert md5(Path(td) / "data.bin") == m["data_bin_md5"], name
     print("ok")
 
 
 if __name__ == "__main__":
-    {"fasta": make_fasta, "check": check}[sys.argv[1] if len(sys.argv) > 1 else "check"]()
+    cmd = sys.argv[1] if len(sys.argv) > 1 else "check"
+    if cmd == "fasta":
+        make_fasta(sys.argv[2:] or None)
+    else:
+        check()

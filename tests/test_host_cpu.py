@@ -85,12 +85,18 @@ def _md5(p: Path) -> str:
     return hashlib.md5(p.read_bytes()).hexdigest()
 
 
+def _fixture_fasta(name: str, m: dict, workdir: Path) -> Path:
+    from tests.golden.make_golden import fixture_fasta
+
+    return fixture_fasta(name, m, workdir)
+
+
 def test_makedb_matches_golden_md5(tmp_path):
     manifest = json.loads((GOLDEN / "manifest.json").read_text())
     for name, m in manifest.items():
         d = tmp_path / name
         d.mkdir()
-        ngia.makedb(str(GOLDEN / f"{name}.fasta"), str(d), m["type"])
+        ngia.makedb(str(_fixture_fasta(name, m, d)), str(d), m["type"])
         assert _md5(d / "data.bin") == m["data_bin_md5"], name
         assert (d / "data.fasta").is_symlink()
 
@@ -191,7 +197,7 @@ def test_oracle_matches_reference_golden(tmp_path):
     for name, m in manifest.items():
         d = tmp_path / name
         d.mkdir()
-        ngia.makedb(str(GOLDEN / f"{name}.fasta"), str(d), m["type"])
+        ngia.makedb(str(_fixture_fasta(name, m, d)), str(d), m["type"])
         for s, w, p in m["params"]:
             tag = f"s{s}_w{w}_p{p}"
             exp = ref_root / name / tag
@@ -201,10 +207,37 @@ def test_oracle_matches_reference_golden(tmp_path):
             od.mkdir()
             subprocess.run([str(ROOT / "oracle" / "_build" / "ngia_oracle"), "-i", str(d), "-o", str(od), "-w",
                             str(w), "-s", str(s), "-p", str(p)], check=True, capture_output=True)
-            for f in ("cluster.txt", "represent.fasta"):
-                assert (od / f).read_bytes() == (exp / f).read_bytes(), f"{name}/{tag}/{f}"
+            if (exp / "outputs.json").exists():  # generated fixture: outputs pinned by md5
+                want = json.loads((exp / "outputs.json").read_text())
+                for f in ("cluster.txt", "represent.fasta"):
+                    assert _md5(od / f) == want[f], f"{name}/{tag}/{f}"
+            else:
+                for f in ("cluster.txt", "represent.fasta"):
+                    assert (od / f).read_bytes() == (exp / f).read_bytes(), f"{name}/{tag}/{f}"
             checked += 1
     assert checked > 0
+
+
+def test_q1_fixture_exercises_the_thread_return(tmp_path):
+    """On the dna_q1 fixture the reference's short-word kernel has more jobs
+    than threads in the first iteration: the records at list position
+    p + 16384 of a short record's position p join the first representative
+    although the short-word test, run on the pair, rejects them; the same
+    records elsewhere in the list stay out."""
+    from tests.golden import q1_fixture
+
+    seqs, facts = q1_fixture.records()
+    db = seqs_to_db(0, seqs)
+    assert db.n == len(seqs) and db.read_len[0] == 25 and (db.read_len[1:] == 16).all()
+    for s, w, p in q1_fixture.PARAMS:
+        cl, _, st = oracle.cluster(db.words, db.rec_off, 0, s, w, p)
+        assert st["candidates"] > 0
+        for pos in facts["skipped_pos"] + facts["control_pos"]:
+            out = oracle.pair(db.words, db.rec_off, 0, s, w, 0, pos)
+            assert out[4] == 1 and out[5] == 0 and out[6] == 1  # composition ok, words rejected, LCS ok
+        assert all(cl[pos] == 0 for pos in facts["skipped_pos"])
+        assert not any(cl[pos] == 0 for pos in facts["control_pos"])
+        assert all(db.words[db.rec_off[pos] + 1] == 15 for pos in facts["short_pos"])
 
 
 # ---- oracle known answers --------------------------------------------------
