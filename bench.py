@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--iters-per-step", type=int, default=32)
     ap.add_argument("--similarity", type=float, default=0.85)
     ap.add_argument("--word", type=int, default=5)
-    ap.add_argument("--workload", default="dna_1m", help="dna_small | dna_1m | protein_200k | batch256 | serve")
+    ap.add_argument("--workload", default="dna_1m",
+                    help="dna_small | dna_1m | protein_200k | batch256 | serve | dna_1m_whole")
     ap.add_argument("--batch-jobs", type=int, default=256)
     ap.add_argument("--batch-max-seqs", type=int, default=200000)
     ap.add_argument("--serve-batches", type=int, default=200)
@@ -65,9 +66,17 @@ def parse():
     ap.add_argument("--skip-e2e", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-drivers", action="store_true", help="skip the whole-job graph vs plain comparison")
+    ap.add_argument("--skip-secondary", action="store_true",
+                    help="skip the sub-results of the other configurations (protein, serving, reference GPU)")
     ap.add_argument("--autotune", type=int, default=4, help="iterations per setting tried by ngia_autotune (0: off)")
-    ap.add_argument("--sweep", default="", help="comma-separated similarities to time as well (e.g. 0.8,0.85,0.9)")
-    ap.add_argument("--sweep-steps", type=int, default=3)
+    ap.add_argument("--sweep", default="0.8,0.9,0.95,0.99",
+                    help="comma-separated similarities to time as well ('' = none)")
+    ap.add_argument("--sweep-steps", type=int, default=2)
+    ap.add_argument("--whole-mode", default="spec", choices=["spec", "graph", "plain"],
+                    help="dna_1m_whole: the driver form that runs the whole job")
+    ap.add_argument("--whole-chunk", type=int, default=8192, help="dna_1m_whole: representatives per step call")
+    ap.add_argument("--whole-probe", type=int, default=64,
+                    help="dna_1m_whole: iterations of each form timed from every checkpoint")
     ap.add_argument("--cpu-only", action="store_true",
                     help="replica plumbing with the CPU oracle as the engine (tests; no GPU)")
     return ap.parse_args()
@@ -151,6 +160,17 @@ class Clocks:
                 "power_w_max": max(r[2] for r in rows), "samples": len(rows), "reasons": reasons}
 
 
+def repo_libraries() -> list[str]:
+    """Shared libraries of this repository mapped into the process."""
+    try:
+        maps = Path("/proc/self/maps").read_text().splitlines()
+    except OSError:
+        return []
+    root = str(ROOT)
+    return sorted({ln.split()[-1][len(root) + 1:] for ln in maps
+                   if ln.split()[-1].startswith(root) and ".so" in ln.split()[-1]})
+
+
 def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -188,19 +208,30 @@ def workload_desc(args, cfg, db_bytes: int | None = None) -> dict:
 
 # ---- reference arm: the oracle on the host cores ---------------------------------
 def run_reference(args, dist: Dist):
+    """The reference algorithm's CPU restatement (the oracle) on all host
+    cores.  Its inputs come from oracle-side code only: the seeded generator
+    built on its own (oracle/_build/libsynth.so), the oracle's restatement of
+    makeDB's packing and of readIndex's clamps; the product library is not
+    loaded in this arm."""
     if dist.rank != 0:
         return
-    from oracle import oracle
-    import ngia
+    import platform
 
-    db, cfg = make_db(args)
-    p = ngia.params_clamp(cfg["type"], args.similarity, args.word, 0)
+    from oracle import oracle
+    from ngia import CONFIGS  # the workload table (importing it loads no library)
+
+    cfg = dict(CONFIGS[args.workload])
+    if args.n_seqs:
+        cfg["n_seqs"] = args.n_seqs
+    seq, off = oracle.synth(seed=args.seed, **cfg)
+    words, rec_off = oracle.pack(cfg["type"], seq, off)
+    del seq
+    s, w, prec = oracle.clamp(cfg["type"], args.similarity, args.word, 0)
     cores = os.cpu_count() or 1
     times, cands = [], []
     for k in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        _, _, st = oracle.cluster(db.words, db.rec_off, cfg["type"], p.similarity, p.word_length, p.precise,
-                                  threads=0, max_iters=1)
+        _, _, st = oracle.cluster(words, rec_off, cfg["type"], s, w, prec, threads=0, max_iters=1)
         dt = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(dt)
@@ -211,193 +242,310 @@ def run_reference(args, dist: Dist):
            "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u32", "impl": "reference",
            "data": "synthetic (seeded generator with the configuration's shapes)",
-           "config": {**workload_desc(args, cfg, db.words.nbytes), "iters_per_step": 1},
-           "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                            "sample": f"first greedy iteration (representative vs all {db.n:,} sequences) per step"},
-           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+           "config": {**workload_desc(args, cfg, words.nbytes), "iters_per_step": 1},
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "arch": platform.machine(), "kind": "port",
+                            "sample": f"first greedy iteration (representative vs all {len(rec_off):,} sequences) "
+                                      f"per step, C/OpenMP restatement of the reference on all host threads"},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "libraries": repo_libraries()}
     print(json.dumps(out), flush=True)
 
 
 # ---- our arm ------------------------------------------------------------------------
+def stage_replay(ctx, ck: str, iters: int) -> dict:
+    """Resumes the checkpoint taken at the start of the timed region in the
+    plain driver with CUDA events around every stage launch on the library
+    stream and runs the same `iters` greedy iterations again; returns the
+    stage times and the work counters of exactly those iterations, and the
+    assignment they end with."""
+    import ngia
+
+    ctx.resume(ck, ngia.MODE_PLAIN)
+    a = ctx.stats()
+    ctx.set_profiling(True)
+    ctx.step(iters)
+    ctx.set_profiling(False)
+    cl, ident, b = ctx.end()
+    d = {k: (b[k] - a[k]) for k in ("iterations", "candidates", "band_cells", "done_cells", "filter_bytes",
+                                    "align_pairs")}
+    d["ms_filter"], d["ms_align"] = b["ms_filter"], b["ms_align"]  # the resumed run starts its timers at 0
+    for k in ("class_pairs", "class_cells", "class_bytes"):
+        d[k] = [y - x for x, y in zip(a[k], b[k])]
+    d["class_ms"] = list(b["class_ms"])
+    return d, cl, ident
+
+
+def align_roofline(rep: dict, db_type: int, int_gops: float, ms_per_step: float, S: int) -> dict:
+    """Roofline of the dominant alignment kernel from the replay of the timed
+    iterations: in-band cells it computed / its event time, against the INT32
+    issue rate x 32 cells / the instructions of one 32-cell update."""
+    import ngia
+
+    it = max(1, rep["iterations"])
+    k = max(range(len(rep["class_ms"])), key=lambda i: rep["class_ms"][i])
+    ms_k = rep["class_ms"][k]
+    achieved = rep["class_cells"][k] / (ms_k * 1e-3) / 1e9 if ms_k > 0 else 0.0
+    # DNA reads the match word from the representative's match table (AND,
+    # add with carry, LOP3); protein builds it from 5 planes (5 LOP3, add, LOP3)
+    ops = 3 if db_type == 0 else 7
+    peak = int_gops * 32.0 / ops
+    names = ngia.class_kernels(db_type)
+    return {"bound": "int32", "kernel": names[k], "class": k, "achieved": achieved, "peak": peak, "unit": "Gcell/s",
+            "frac": achieved / peak if peak else None,
+            "traffic": rep["class_bytes"][k] / it,
+            "traffic_kind": "algorithmic bytes per launch (query planes of the pairs the launch aligns; the "
+                            "representative's planes are staged once per CTA); one launch per iteration",
+            "ms_per_launch": ms_k / it, "launch_ms_per_step": ms_k / it * S, "ms_per_step": ms_per_step,
+            "launch_within_step": ms_k / it * S <= ms_per_step, "share_of_step": ms_k / it * S / ms_per_step,
+            "peak_source": f"of measured INT32 issue rate {int_gops:.0f} Gop/s (probe, same LOP3/IADD3 mix) x 32 "
+                           f"cells / {ops} ops",
+            "pairs_per_launch": rep["class_pairs"][k] / it,
+            "reference_cells_rate": rep["band_cells"] / (rep["ms_align"] * 1e-3) / 1e9 if rep["ms_align"] else None,
+            "replayed_iterations": it, "ms_align_per_iter": rep["ms_align"] / it,
+            "class_ms_per_iter": [round(x / it, 4) for x in rep["class_ms"]],
+            "class_pairs_per_iter": [round(x / it) for x in rep["class_pairs"]],
+            "how": "the timed region starts from a checkpoint; its iterations are replayed from that checkpoint in "
+                   "the plain driver with CUDA events around each stage launch (assignments identical)"}
+
+
+def filter_roofline(rep: dict, peaks: dict) -> dict:
+    it = max(1, rep["iterations"])
+    ms = rep["ms_filter"]
+    gbs = rep["filter_bytes"] / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+    return {"bound": "hbm", "kernel": "k_prep + k_filter", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+            "frac": gbs / peaks["hbm_gbs"], "traffic": rep["filter_bytes"] / it, "peak_source": peaks["source"],
+            "traffic_kind": "algorithmic filter bytes per iteration (headers of every candidate, planes of the "
+                            "word-tested ones)", "ms_filter_per_iter": ms / it}
+
+
+def timed_run(args, dist, db, cfg, p, S: int, steps: int, warmup: int, autotune: int, clocks: bool = True):
+    """Tuning, warm-up, then `steps` timed steps of S greedy iterations in the
+    graph driver (device time on the library stream) from a checkpoint, and
+    the stage replay of the same iterations."""
+    import numpy as np
+
+    import ngia
+
+    ctx = ngia.Context(db)
+    tuning = ctx.autotune(p, autotune) if autotune > 0 else None  # before the timed region
+    ctx.begin(p, ngia.MODE_GRAPH)
+    for _ in range(warmup):
+        ctx.step(S)
+    with tempfile.TemporaryDirectory() as td:
+        ck = os.path.join(td, "timed.ckpt")
+        ctx.save(ck)  # the state the timed region starts from (outside the timing)
+        dist.barrier()
+        st0 = ctx.stats()
+        clk = Clocks(dist.local) if clocks else None
+        if clk:
+            clk.start()
+        t_wall = time.perf_counter()
+        dev_ms = 0.0
+        for _ in range(steps):
+            ctx.step(S)
+            dev_ms += ctx.step_ms()
+        t_wall = time.perf_counter() - t_wall
+        clk_out = clk.stop() if clk else None
+        st1 = ctx.stats()
+        dist.barrier()
+        cl_t, id_t, _ = ctx.end()
+        rep, cl_r, id_r = stage_replay(ctx, ck, S * steps)
+    ctx.close()
+    return {"tuning": tuning, "dev_ms": dev_ms, "t_wall": t_wall, "clocks": clk_out,
+            "cands": st1["candidates"] - st0["candidates"], "cells": st1["band_cells"] - st0["band_cells"],
+            "iters": st1["iterations"] - st0["iterations"], "replay": rep,
+            "replay_identical": bool(np.array_equal(cl_t, cl_r) and np.array_equal(id_t, id_r))}
+
+
 def run_ours(args, dist: Dist):
     import ngia
 
     ngia.set_device(dist.local)
     db, cfg = make_db(args)
     p = ngia.params_clamp(cfg["type"], args.similarity, args.word, 0)
-    mode = ngia.MODE_GRAPH if args.mode == "graph" else ngia.MODE_PLAIN
     S = args.iters_per_step
-    # per iteration: prep, filter, next, and per class the thread-per-pair and
-    # the warp-per-pair kernel
-    launches_per_iter = 3 + 2 * ngia_classes(cfg["type"])
     int_gops = ngia.measure_int_peak() if dist.rank == 0 else 0.0
-
-    ctx = ngia.Context(db)
-    tuning = ctx.autotune(p, args.autotune) if args.autotune > 0 else None  # before the timed region
-    # short words first with records over 2,048 residues: k_filter_long too
+    r = timed_run(args, dist, db, cfg, p, S, args.steps, args.warmup, args.autotune)
+    T = dist.reduce(r["dev_ms"] / 1e3, "max")
+    total_cands = dist.reduce(float(r["cands"]), "sum")
+    total_cells = dist.reduce(float(r["cells"]), "sum")
+    tuning = r["tuning"]
+    # per iteration: prep, filter, next, and per class the thread-per-pair and
+    # the warp-per-pair kernel; k_filter_long when short words go first and
+    # records exceed 2,048 residues
+    launches_per_iter = 3 + 2 * ngia_classes(cfg["type"])
     wo = tuning["word_order"] if tuning else 0
     word_first = wo == 1 or (wo == 0 and (cfg["type"] == 1 or p.similarity >= 0.93))
     if word_first and not p.precise and int(db.words[db.rec_off + 1].max()) > 2048:
         launches_per_iter += 1
-    ctx.begin(p, mode)
-    for _ in range(args.warmup):
-        ctx.step(S)
-    dist.barrier()
-    st0 = ctx.stats()
-    clocks = Clocks(dist.local)
-    clocks.start()
-    t_wall = time.perf_counter()
-    dev_ms = 0.0
-    for _ in range(args.steps):
-        ctx.step(S)
-        dev_ms += ctx.step_ms()
-    t_wall = time.perf_counter() - t_wall
-    clk = clocks.stop()
-    st1 = ctx.stats()
-    dist.barrier()
-    cands = st1["candidates"] - st0["candidates"]
-    cells = st1["band_cells"] - st0["band_cells"]
-    T = dist.reduce(dev_ms / 1e3, "max")
-    total_cands = dist.reduce(float(cands), "sum")
-    total_cells = dist.reduce(float(cells), "sum")
-
-    # stage timings (plain driver, CUDA events around the filter and alignment
-    # launches on their stream) for the rooflines
-    ctx.begin(p, ngia.MODE_PLAIN)
-    ctx.step(2)
-    a = ctx.stats()
-    ctx.set_profiling(True)
-    ctx.step(max(4, S // 4))
-    b = ctx.stats()
-    ctx.set_profiling(False)
-    ms_align, ms_filter = b["ms_align"], b["ms_filter"]
-    prof_iters = b["iterations"] - a["iterations"]
-    done_gcell = (b["done_cells"] - a["done_cells"]) / (ms_align * 1e-3) / 1e9
-    band_gcell = (b["band_cells"] - a["band_cells"]) / (ms_align * 1e-3) / 1e9
-    filt_gbs = (b["filter_bytes"] - a["filter_bytes"]) / (ms_filter * 1e-3) / 1e9
-    ctx.close()
-
-    # whole jobs: the 20,000-sequence DNA configuration clustered to the end by
-    # the device-side graph driver and by the plain host loop
-    drivers = None
-    if dist.rank == 0 and not args.skip_drivers:
-        import numpy as np
-
-        small_cfg = dict(ngia.CONFIGS["dna_small"])
-        sq = ngia.synth(**small_cfg, seed=args.seed)
-        sdb = ngia.DB.pack(0, sq, sq.off)
-        sq.close()
-        sp = ngia.params_clamp(0, args.similarity, args.word, 0)
-        times, outs = {}, {}
-        with ngia.Context(sdb) as sctx:
-            for name, mode in (("graph", ngia.MODE_GRAPH), ("plain", ngia.MODE_PLAIN), ("spec", ngia.MODE_SPEC)):
-                sctx.cluster(sp, mode)  # warm-up (graph capture, caches, buffers)
-                t0 = time.perf_counter()
-                outs[name] = sctx.cluster(sp, mode)
-                times[name] = time.perf_counter() - t0
-        same = all(np.array_equal(a, b) for name in ("plain", "spec")
-                   for a, b in zip(outs["graph"][:2], outs[name][:2]))
-        drivers = {"workload": f"dna_small: {sdb.n:,} DNA sequences (400 ancestors) clustered to the end, "
-                               f"s={args.similarity}, w={args.word}",
-                   "representatives": int(outs["graph"][2]["iterations"]),
-                   "graph_s": times["graph"], "plain_s": times["plain"], "spec_s": times["spec"],
-                   "graph_seqs_per_s": sdb.n / times["graph"], "plain_seqs_per_s": sdb.n / times["plain"],
-                   "spec_seqs_per_s": sdb.n / times["spec"],
-                   "speedup": times["plain"] / times["graph"], "spec_speedup_vs_plain": times["plain"] / times["spec"],
-                   "identical": bool(same),
-                   "forms": "graph: device-side driver, one representative per iteration; plain: host loop, one "
-                            "launch sequence per representative; spec: speculative rounds of up to 64 "
-                            "candidate representatives once the unclustered set is small",
-                   "timing": "host clock around ngia_cluster (assignment and scores returned)"}
-        sdb.close()
-
-    # similarity sweep of the same database (configuration 2 lists s = 0.80,
-    # 0.85, 0.90, 0.95, 0.99): tuned, then timed over a few steps each
-    sweep = None
-    if dist.rank == 0 and args.sweep:
-        sweep = []
-        for sv in (float(x) for x in args.sweep.split(",")):
-            sp = ngia.params_clamp(cfg["type"], sv, args.word, 0)
-            with ngia.Context(db) as sctx:
-                tun = sctx.autotune(sp, args.autotune) if args.autotune > 0 else None
-                sctx.begin(sp, ngia.MODE_GRAPH)
-                sctx.step(S)
-                a0 = sctx.stats()
-                ms = 0.0
-                for _ in range(args.sweep_steps):
-                    sctx.step(S)
-                    ms += sctx.step_ms()
-                a1 = sctx.stats()
-            sweep.append({"similarity": sv, "word_length": sp.word_length,
-                          "value": (a1["candidates"] - a0["candidates"]) / (ms * 1e-3),
-                          "gcups": (a1["band_cells"] - a0["band_cells"]) / (ms * 1e-3) / 1e9,
-                          "ms_per_iteration": ms / (args.sweep_steps * S),
-                          "tuning": {k: tun[k] for k in ("word_order", "refill", "warp_pairs")} if tun else None})
 
     out = None
     if dist.rank == 0:
-        # INT32 operations per 32-cell word step: DNA reads the match word from
-        # the representative's match table (AND, add with carry, LOP3);
-        # protein builds it from 5 planes (one LOP3 per plane, add, LOP3)
-        ops = 3 if cfg["type"] == 0 else 7
-        peak_gcell = int_gops * 32.0 / ops
         peaks = measured_peaks()
-        e2e = None
-        if not args.skip_e2e:
-            e2e = run_e2e(args, db, p, S)
+        ms_per_step = 1e3 * T / args.steps
+        roof = align_roofline(r["replay"], cfg["type"], int_gops, ms_per_step, S)
+        froof = filter_roofline(r["replay"], peaks)
+        drivers = None if args.skip_drivers or dist.world > 1 else whole_job_drivers(args)
+        sweep = similarity_sweep(args, db, cfg) if args.sweep and dist.world == 1 else None
+        e2e = None if args.skip_e2e else run_e2e(args, db, p, S)
         cpu = None
         if not args.skip_cpu and dist.world == 1:
             cpu = run_cpu_baseline(args, db, p, cfg)
+        secondary = None if args.skip_secondary or dist.world > 1 else run_secondary(args, dist, int_gops, peaks)
         out = {"metric": METRIC, "value": total_cands / T, "unit": UNIT, "n_gpus": dist.world,
-               "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
+               "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
                "data": "synthetic (seeded generator with the configuration's shapes)",
                "config": workload_desc(args, cfg, db.words.nbytes),
                "gcups": total_cells / T / 1e9,
                "gcups_note": "reference band cells (func.cu loop bounds) of the pairs aligned, per second",
-               "wall_s_timed": t_wall,
-               "roofline": {"bound": "int32", "kernel": "k_align_* (banded bit-parallel LCS)",
-                            "achieved": done_gcell, "peak": peak_gcell, "unit": "Gcell/s",
-                            "frac": done_gcell / peak_gcell if peak_gcell else None,
-                            "traffic": profiled_traffic(args),
-                            "traffic_note": "DRAM bytes per launch of k_align_tiled<2,64> from one ncu capture "
-                                            "(profiles/align_tiled_dna_1m.md); algorithmic: the query planes "
-                                            "of ~995k pairs, ~390 MB",
-                            "peak_source": f"of measured INT32 issue rate {int_gops:.0f} Gop/s (probe) x 32 cells"
-                                           f" / {ops} ops", "reference_cells_rate": band_gcell,
-                            "profiled_iterations": prof_iters, "ms_align_per_iter": ms_align / prof_iters,
-                            "class_ms_per_iter": [round((y - x) / prof_iters, 3) for x, y in
-                                                  zip(a["class_ms"], b["class_ms"])],
-                            "class_pairs_per_iter": [round((y - x) / prof_iters) for x, y in
-                                                     zip(a["class_pairs"], b["class_pairs"])]},
-               "filter_roofline": {"bound": "hbm", "kernel": "k_prep + k_filter", "achieved": filt_gbs,
-                                   "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                                   "frac": filt_gbs / peaks["hbm_gbs"], "traffic": None,
-                                   "peak_source": peaks["source"],
-                                   "ms_filter_per_iter": ms_filter / prof_iters},
+               "wall_s_timed": r["t_wall"], "iterations_timed": r["iters"],
+               "roofline": roof, "filter_roofline": froof, "replay_identical": r["replay_identical"],
                "gpu_launches": launches_per_iter * S * args.steps,
-               "drivers_whole_job": drivers,
-               "tuning": tuning,
-               "similarity_sweep": sweep,
-               "clocks": clk, "cpu_baseline": cpu, "e2e": e2e}
+               "drivers_whole_job": drivers, "tuning": tuning, "similarity_sweep": sweep,
+               "secondary": secondary, "clocks": r["clocks"], "cpu_baseline": cpu, "e2e": e2e,
+               "libraries": repo_libraries()}
     db.close()
     if out is not None:
         print(json.dumps(out), flush=True)
 
 
-def profiled_traffic(args) -> int | None:
-    """DRAM bytes per launch of the dominant alignment kernel from the
-    committed ncu summary, when it was captured on this workload."""
-    path = ROOT / "profiles" / "align_tiled_dna_1m.md"
+def whole_job_drivers(args) -> dict:
+    """The 20,000-sequence DNA configuration clustered to the end by the
+    device-side graph driver, the plain host loop and the speculative rounds
+    (host clock around ngia_cluster; assignment and scores returned)."""
+    import numpy as np
+
+    import ngia
+
+    small_cfg = dict(ngia.CONFIGS["dna_small"])
+    sq = ngia.synth(**small_cfg, seed=args.seed)
+    sdb = ngia.DB.pack(0, sq, sq.off)
+    sq.close()
+    sp = ngia.params_clamp(0, args.similarity, args.word, 0)
+    times, outs = {}, {}
+    with ngia.Context(sdb) as sctx:
+        for name, mode in (("graph", ngia.MODE_GRAPH), ("plain", ngia.MODE_PLAIN), ("spec", ngia.MODE_SPEC)):
+            sctx.cluster(sp, mode)  # warm-up (graph capture, caches, buffers)
+            t0 = time.perf_counter()
+            outs[name] = sctx.cluster(sp, mode)
+            times[name] = time.perf_counter() - t0
+    same = all(np.array_equal(a, b) for name in ("plain", "spec") for a, b in zip(outs["graph"][:2], outs[name][:2]))
+    out = {"workload": f"dna_small: {sdb.n:,} DNA sequences (400 ancestors) clustered to the end, "
+                       f"s={args.similarity}, w={args.word}",
+           "representatives": int(outs["graph"][2]["iterations"]),
+           "graph_s": times["graph"], "plain_s": times["plain"], "spec_s": times["spec"],
+           "graph_seqs_per_s": sdb.n / times["graph"], "plain_seqs_per_s": sdb.n / times["plain"],
+           "spec_seqs_per_s": sdb.n / times["spec"],
+           "speedup": times["plain"] / times["graph"], "spec_speedup_vs_plain": times["plain"] / times["spec"],
+           "identical": bool(same),
+           "forms": "graph: device-side driver, one representative per iteration; plain: host loop, one launch "
+                    "sequence per representative; spec: speculative rounds of up to 64 candidate representatives "
+                    "once the unclustered set is small",
+           "timing": "host clock around ngia_cluster (assignment and scores returned)"}
+    sdb.close()
+    return out
+
+
+def similarity_sweep(args, db, cfg) -> list:
+    """The same database at the other similarities of its configuration:
+    tuned, then timed over a few steps each (graph driver, device time)."""
+    import ngia
+
+    S = args.iters_per_step
+    out = []
+    for sv in (float(x) for x in args.sweep.split(",")):
+        sp = ngia.params_clamp(cfg["type"], sv, args.word, 0)
+        with ngia.Context(db) as sctx:
+            tun = sctx.autotune(sp, args.autotune) if args.autotune > 0 else None
+            sctx.begin(sp, ngia.MODE_GRAPH)
+            sctx.step(S)
+            a0 = sctx.stats()
+            ms = 0.0
+            for _ in range(args.sweep_steps):
+                sctx.step(S)
+                ms += sctx.step_ms()
+            a1 = sctx.stats()
+        out.append({"similarity": sv, "word_length": sp.word_length,
+                    "value": (a1["candidates"] - a0["candidates"]) / (ms * 1e-3),
+                    "gcups": (a1["band_cells"] - a0["band_cells"]) / (ms * 1e-3) / 1e9,
+                    "ms_per_iteration": ms / (args.sweep_steps * S),
+                    "iterations": f"{S + 1}-{S * (1 + args.sweep_steps)} of a fresh run",
+                    "tuning": {k: tun[k] for k in ("word_order", "refill", "warp_pairs")} if tun else None})
+    return out
+
+
+def run_secondary(args, dist, int_gops: float, peaks: dict) -> dict:
+    """Bounded sub-results of the other configurations, in the same run:
+    the 200k-protein workload at s=0.9 (value and alignment roofline), the
+    serving loop (latency, capacity, oracle replay) and the reference's own
+    CUDA program beside the drop-in tool on the 20,000-sequence DNA
+    configuration (whole program, outputs byte-compared)."""
+    import ngia
+
+    out = {}
+    t0 = time.perf_counter()
     try:
-        text = path.read_text()
-    except OSError:
-        return None
-    fields = dict(line.split(": ", 1) for line in text.splitlines() if line.startswith("traffic_"))
-    want = f"{args.workload} s={args.similarity:g} w={args.word}"
-    if fields.get("traffic_workload") != want:
-        return None
-    return int(fields["traffic_bytes_per_launch"])
+        pa = argparse.Namespace(**{**vars(args), "workload": "protein_200k", "similarity": 0.9, "word": 5,
+                                   "n_seqs": 0})
+        pdb, pcfg = make_db(pa)
+        pp = ngia.params_clamp(1, 0.9, 5, 0)
+        r = timed_run(pa, dist, pdb, pcfg, pp, args.iters_per_step, 3, 2, args.autotune, clocks=False)
+        ms = r["dev_ms"] / 3
+        out["protein_200k"] = {"workload": workload_desc(pa, pcfg, pdb.words.nbytes)["workload"],
+                               "value": r["cands"] / (r["dev_ms"] * 1e-3), "unit": UNIT, "ms_per_step": ms,
+                               "iterations_timed": r["iters"], "gcups": r["cells"] / (r["dev_ms"] * 1e-3) / 1e9,
+                               "roofline": align_roofline(r["replay"], 1, int_gops, ms, args.iters_per_step),
+                               "filter_roofline": filter_roofline(r["replay"], peaks),
+                               "dominant": ("filter" if r["replay"]["ms_filter"] > max(r["replay"]["class_ms"])
+                                            else "alignment"),
+                               "replay_identical": r["replay_identical"], "tuning": r["tuning"]}
+        pdb.close()
+    except Exception as e:  # a sub-result never takes the headline down
+        out["protein_200k"] = {"error": repr(e)}
+    out["protein_200k_s"] = round(time.perf_counter() - t0, 1)
+    t0 = time.perf_counter()
+    try:
+        sa = argparse.Namespace(**{**vars(args), "similarity": 0.9, "word": 5, "cpu_seconds": 10.0,
+                                   "warmup": 3})
+        out["serve"] = serve_summary(run_serve(sa, dist, emit=False))
+    except Exception as e:
+        out["serve"] = {"error": repr(e)}
+    out["serve_s"] = round(time.perf_counter() - t0, 1)
+    t0 = time.perf_counter()
+    out["reference_gpu"] = reference_gpu_compare(args)
+    out["reference_gpu_s"] = round(time.perf_counter() - t0, 1)
+    return out
+
+
+def serve_summary(r: dict) -> dict:
+    keep = ("value", "unit", "latency_ms", "offered_batches_per_s", "achieved_batches_per_s", "capacity",
+            "identical_open_loop_and_saturated", "oracle_replay", "gcups", "pairs_aligned")
+    return {"workload": r["config"]["workload"], "slots": r["config"]["slots"],
+            **{k: r[k] for k in keep if k in r}}
+
+
+def reference_gpu_compare(args) -> dict:
+    """The reference's own CUDA clustering program (built from its sources
+    for sm_103a by oracle/ref_cluster.py into baseline/_ref) and the drop-in
+    `cluster` tool on the 20,000-sequence DNA configuration: whole-program
+    wall time each (database load and result writing included) and a byte
+    comparison of cluster.txt / represent.fasta."""
+    stage = ROOT / "baseline" / "_ref" / "signalNode" / "src" / "func.cu"
+    if not stage.exists():
+        return {"unavailable": "the reference's sources are not staged in baseline/_ref/signalNode"}
+    try:
+        from oracle import ref_cluster
+
+        with tempfile.TemporaryDirectory() as td:
+            res = ref_cluster.compare(td, "dna_small", args.similarity, args.word, seed=args.seed, quiet=True)
+        ref, ours = res.get("reference", {}), res.get("ours", {})
+        if ref.get("seconds") and ours.get("seconds"):
+            res["speedup"] = ref["seconds"] / ours["seconds"]
+            res["n_seqs_per_s"] = {"reference": res["n_seqs"] / ref["seconds"], "ours": res["n_seqs"] / ours["seconds"]}
+        return res
+    except Exception as e:
+        return {"error": repr(e)}
 
 
 def ngia_classes(db_type: int) -> int:
@@ -483,6 +631,101 @@ def run_cpu_replicas(args, dist: Dist):
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / args.steps,
                           "higher_is_better": True, "scaling": "weak", "cpu_only": True,
                           "config": workload_desc(args, cfg)}), flush=True)
+
+
+# ---- the whole 1M job ------------------------------------------------------------------
+def run_whole(args, dist: Dist):
+    """The 1,000,000-sequence DNA configuration clustered to the end by one
+    driver form (--mode; speculative rounds by default, the form the drop-in
+    `cluster` tool runs): sequences / wall time of the whole job.  Along the
+    way the run is checkpointed when 0, 25, 50, 75 and 95% of the sequences
+    are clustered; from each checkpoint the plain, graph and speculative
+    forms then run the next --whole-probe iterations (timed on the host clock,
+    assignments compared).  The plain form's whole-job time is estimated by
+    scaling each stretch of the measured run by the plain/measured time ratio
+    at the checkpoints around it."""
+    import numpy as np
+
+    import ngia
+
+    if dist.rank != 0:
+        return
+    args.workload = "dna_1m"
+    db, cfg = make_db(args)
+    p = ngia.params_clamp(0, args.similarity, args.word, 0)
+    forms = {"plain": ngia.MODE_PLAIN, "graph": ngia.MODE_GRAPH, "spec": ngia.MODE_SPEC}
+    main = forms[args.whole_mode]
+    marks = [0.0, 0.25, 0.5, 0.75, 0.95]
+    ctx = ngia.Context(db)
+    tuning = ctx.autotune(p, args.autotune) if args.autotune > 0 else None
+    clocks = Clocks(dist.local)
+    with tempfile.TemporaryDirectory() as td:
+        cks, seg = [], []
+        ctx.begin(p, main)
+        wall = dev = 0.0
+        done, k, curve = False, 0, []
+        clocks.start()
+        while True:
+            cl, _, st = ctx.end()  # progress (outside the timing)
+            frac = float((cl >= 0).sum()) / db.n
+            while k < len(marks) and frac >= marks[k] and not done:
+                path = os.path.join(td, f"m{k}.ckpt")
+                ctx.save(path)
+                cks.append((marks[k], path, frac, wall, int(st["iterations"])))
+                k += 1
+            curve.append((int(st["iterations"]), round(frac, 4), round(wall, 2)))
+            if done:
+                break
+            t0 = time.perf_counter()
+            done = ctx.step(args.whole_chunk)
+            wall += time.perf_counter() - t0
+            dev += ctx.step_ms()
+        clk = clocks.stop()
+        cl_main, id_main, st_main = ctx.end()
+        reps = int(st_main["iterations"])
+        # the forms side by side from every checkpoint
+        probes = []
+        for mark, path, frac, w_at, it_at in cks:
+            res, outs = {}, {}
+            for name, mode in forms.items():
+                ctx.resume(path, mode)
+                t0 = time.perf_counter()
+                ctx.step(args.whole_probe)
+                dt = time.perf_counter() - t0
+                cl, ident, st = ctx.end()
+                outs[name] = (cl, ident)
+                res[name] = {"ms_per_iteration": 1e3 * dt / max(1, int(st["iterations"]) - it_at),
+                             "iterations": int(st["iterations"]) - it_at}
+            same = all(np.array_equal(outs["plain"][0], outs[f][0]) and np.array_equal(outs["plain"][1], outs[f][1])
+                       for f in forms)
+            probes.append({"mark": mark, "clustered": round(frac, 4), "unclustered": int(round((1 - frac) * db.n)),
+                           "representatives_before": it_at, "wall_s_at": round(w_at, 2), "forms": res,
+                           "identical": bool(same)})
+    ctx.close()
+    # plain whole-job estimate: each stretch between checkpoints scaled by the
+    # mean plain/measured per-iteration ratio at its two ends
+    ratios = [pr["forms"]["plain"]["ms_per_iteration"] / pr["forms"][args.whole_mode]["ms_per_iteration"]
+              for pr in probes]
+    bounds = [pr["wall_s_at"] for pr in probes] + [wall]
+    est = 0.0
+    for i in range(len(probes)):
+        r = ratios[i] if i + 1 >= len(ratios) else 0.5 * (ratios[i] + ratios[i + 1])
+        est += (bounds[i + 1] - bounds[i]) * r
+    step = max(1, len(curve) // 60)
+    out = {"metric": "seqs/sec (whole clustering job, bit-exact)", "value": db.n / wall, "unit": "seqs/s",
+           "n_gpus": 1, "higher_is_better": True, "dtype": "u32",
+           "data": "synthetic (seeded generator with the configuration's shapes)",
+           "config": {"workload": workload_desc(args, cfg, db.words.nbytes)["workload"], "form": args.whole_mode,
+                      "chunk": args.whole_chunk, "probe_iterations": args.whole_probe},
+           "wall_s": wall, "device_s": dev / 1e3, "representatives": reps,
+           "tuning": tuning, "clocks": clk, "checkpoints": probes,
+           "plain_estimate": {"wall_s": est, "seqs_per_s": db.n / est, "ratio_measured_vs_plain": est / wall,
+                              "how": "each stretch of the measured run between checkpoints scaled by the plain / "
+                                     "measured time per iteration at its ends (mean of the two)"},
+           "progress": curve[::step] + ([curve[-1]] if curve[-1] not in curve[::step] else []),
+           "libraries": repo_libraries()}
+    print(json.dumps(out), flush=True)
+    db.close()
 
 
 # ---- batch workload: many independent jobs -----------------------------------------
@@ -626,7 +869,7 @@ def serve_workload(args):
     return p, res_db, reps, batches, np.cumsum(gaps) - gaps[0]
 
 
-def run_serve(args, dist: Dist):
+def run_serve(args, dist: Dist, emit: bool = True):
     """Serving arm: the batches are submitted at their Poisson arrival times
     by one thread while another collects them; latency = arrival to result
     (queueing included), throughput = queries / (first arrival to last
@@ -717,10 +960,12 @@ def run_serve(args, dist: Dist):
                                                                    np.argsort([b.n for b in batches])[:checked])),
                              "identical": bool(same)},
            "clocks": clk}
-    print(json.dumps(out), flush=True)
     for b in batches:
         b.close()
     res_db.close()
+    if emit:
+        print(json.dumps(out), flush=True)
+    return out
 
 
 def main():
@@ -738,6 +983,8 @@ def main():
             run_batch(args, dist)
         elif args.workload == "serve":
             run_serve(args, dist)
+        elif args.workload == "dna_1m_whole":
+            run_whole(args, dist)
         else:
             run_ours(args, dist)
     finally:

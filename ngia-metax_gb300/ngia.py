@@ -209,6 +209,17 @@ CONFIGS = {
 }
 
 
+def class_kernels(db_type: int) -> list[str]:
+    """Thread-per-pair kernel of each alignment work class (by band window,
+    in 32-residue blocks); every class also launches the warp-per-pair
+    kernel, which does the class's work instead when it has few pairs."""
+    if db_type == 0:
+        return ["k_align_win<2,8>", "k_align_win<2,16>", "k_align_win<2,24>", "k_align_win<2,32>",
+                "k_align_tiled<2,64>", "k_align_tiled<2,128>", "k_align_tiled<2,0>"]
+    return ["k_align_win<5,8>", "k_align_win<5,16>", "k_align_tiled<5,64>", "k_align_tiled<5,128>",
+            "k_align_tiled<5,0>"]
+
+
 class Seqs:
     """Generated residues, owned by the library (no Python-side copy).
 

@@ -3,6 +3,10 @@ own makeDB tool.
 
 * ``oracle/_build/liboracle.so`` and ``oracle/_build/ngia_oracle``: the C
   restatement of the reference clustering (gcc, OpenMP, -ffp-contract=off).
+* ``oracle/_build/libsynth.so``: the seeded workload generator
+  (ngia-metax_gb300/host/synth.cpp, the same source the product library
+  carries) on its own, so that the timed CPU reference arm builds its inputs
+  without loading the product library.
 * ``oracle/_ref/makeDB``: the reference makeDB compiled from its single
   source file where it lies (``makeDB/src/makeDB.cpp`` of the reference
   tree, with its own cmdline.h / timer.h headers), exactly as its Makefile
@@ -16,6 +20,7 @@ import subprocess
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
+ROOT = HERE.parent
 OUT = HERE / "_build"
 REF_OUT = HERE / "_ref"
 REFERENCE = Path(os.environ.get("NGIA_REFERENCE_DIR", "/root/reference"))
@@ -44,6 +49,11 @@ def build_oracle() -> Path:
     exe = OUT / "ngia_oracle"
     if _stale(exe, src + hdr + [HERE / "oracle_main.c"]):
         _run([CC] + CFLAGS + [str(HERE / "oracle_main.c"), str(src[0]), "-o", str(exe), "-lm"])
+    gen_src = [ROOT / "ngia-metax_gb300" / "host" / f for f in ("synth.cpp", "errors.cpp")]
+    gen = OUT / "libsynth.so"
+    if _stale(gen, gen_src + list((ROOT / "ngia-metax_gb300" / "host").glob("*.h")) + [ROOT / "include" / "ngia.h"]):
+        _run([CXX, "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-ffp-contract=off", "-Wl,-Bsymbolic"] +
+             [str(x) for x in gen_src] + ["-o", str(gen)])
     nofma = OUT / "liboracle_nofma.so"  # separately rounded band shift (fixture search only)
     if _stale(nofma, src + hdr):
         _run([CC] + CFLAGS + ["-DORA_BAND_NOFMA", "-fPIC", "-shared", str(src[0]), "-o", str(nofma), "-lm"])

@@ -417,6 +417,93 @@ int64_t ora_assign(const uint32_t *rbuf, const int64_t *roff, int nrep, const ui
   return clusters;
 }
 
+/* ---- makeDB packing (makeDB/src/makeDB.cpp) ---------------------------------
+ * Residue code of one character, -1 for a character the record skips
+ * (counted in the raw length, not in the net length): DNA a c g t/u -> 0..3
+ * (makeDataGen, makeDB.cpp:108-151); protein a..z -> 0..25, '*' -> 26,
+ * '-' -> 27 for lower case and A..Z -> 0..25 for upper case (makeDataPro,
+ * makeDB.cpp:153-252: '*' and '-' appear only in its lower-case branch, and
+ * the upper-case branch has no code for them, so both cases map the same). */
+static int res_code(int type, unsigned char c) {
+  if (type == 0) {
+    switch (c) {
+      case 'a': case 'A': return 0;
+      case 'c': case 'C': return 1;
+      case 'g': case 'G': return 2;
+      case 't': case 'T': case 'u': case 'U': return 3;
+      default: return -1;
+    }
+  }
+  if (c >= 'a' && c <= 'z') return c - 'a';
+  if (c >= 'A' && c <= 'Z') return c - 'A';
+  if (c == '*') return 26;
+  if (c == '-') return 27;
+  return -1;
+}
+
+/* One record: [len, net, counts, planes]; residue k of each 32-residue
+ * block of the net sequence sits at bit k of the block's planes (makeDB
+ * shifts each new residue in from the top and shifts a partial last block
+ * down to bit 0). */
+static void pack_record(int type, const unsigned char *r, int64_t len, uint32_t *out) {
+  const int A = type ? 28 : 4, P = planes(type), hw = hdr_words(type);
+  const int64_t nb = (len + 31) / 32;
+  memset(out, 0, sizeof(uint32_t) * (size_t)(hw + nb * P));
+  int64_t net = 0;
+  for (int64_t i = 0; i < len; i++) {
+    const int c = res_code(type, r[i]);
+    if (c < 0) continue;
+    out[2 + c] += 1;
+    uint32_t *blk = out + hw + (net / 32) * P;
+    for (int p = 0; p < P; p++) blk[p] |= (uint32_t)((c >> p) & 1) << (net % 32);
+    net++;
+  }
+  (void)A;
+  out[0] = (uint32_t)len;
+  out[1] = (uint32_t)net;
+}
+
+int64_t ora_pack(int type, const char *seq, const int64_t *off, int64_t n, uint32_t *words,
+                 int64_t *rec_off, int64_t *n_words) {
+  /* stable counting sort by raw length, longest first */
+  int64_t *cnt = (int64_t *)calloc(65537 + 1, sizeof(int64_t));
+  int64_t kept = 0, total = 0;
+  for (int64_t i = 0; i < n; i++) {
+    const int64_t len = off[i + 1] - off[i];
+    if (len > 65536) continue;
+    cnt[65536 - len]++;
+    kept++;
+    total += hdr_words(type) + (len + 31) / 32 * planes(type);
+  }
+  if (n_words) *n_words = total;
+  if (!words || !rec_off) {
+    free(cnt);
+    return kept;
+  }
+  int64_t *start = (int64_t *)calloc(65537 + 1, sizeof(int64_t));
+  for (int k = 1; k <= 65537; k++) start[k] = start[k - 1] + cnt[k - 1];
+  int64_t *order = (int64_t *)malloc(sizeof(int64_t) * (size_t)(kept ? kept : 1));
+  for (int64_t i = 0; i < n; i++) {
+    const int64_t len = off[i + 1] - off[i];
+    if (len > 65536) continue;
+    order[start[65536 - len]++] = i;
+  }
+  int64_t w = 0;
+  for (int64_t k = 0; k < kept; k++) {
+    rec_off[k] = w;
+    w += hdr_words(type) + (off[order[k] + 1] - off[order[k]] + 31) / 32 * planes(type);
+  }
+#pragma omp parallel for schedule(dynamic, 256)
+  for (int64_t k = 0; k < kept; k++) {
+    const int64_t i = order[k];
+    pack_record(type, (const unsigned char *)seq + off[i], off[i + 1] - off[i], words + rec_off[k]);
+  }
+  free(order);
+  free(start);
+  free(cnt);
+  return kept;
+}
+
 int ora_load(const char *dir, ora_db *db) {
   memset(db, 0, sizeof(*db));
   char path[4096];

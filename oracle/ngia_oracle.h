@@ -72,6 +72,15 @@ int64_t ora_assign(const uint32_t *rbuf, const int64_t *roff, int nrep, const ui
                    const int64_t *qoff, int nq, int type, float s, int w, int precise, int nthreads,
                    int32_t *rep_out, int32_t *ident_out);
 
+/* makeDB's records (makeDB/src/makeDB.cpp:62-106, 108-252) from raw
+ * sequences given in FASTA order (seq[off[i] .. off[i+1])): records longer
+ * than 65,536 residues are dropped, the rest stable-sorted by raw length,
+ * longest first, and packed.  Called with words == NULL it only returns the
+ * record count and word count (*n_words); then again with words[n_words]
+ * and rec_off[count] to fill them.  Returns the record count. */
+int64_t ora_pack(int type, const char *seq, const int64_t *off, int64_t n, uint32_t *words,
+                 int64_t *rec_off, int64_t *n_words);
+
 /* saveResult (func.cu:680-764): writes cluster.txt and represent.fasta. */
 int ora_save(const char *dbdir, const char *outdir, const ora_db *db, const int32_t *cluster,
              int32_t *n_clusters);

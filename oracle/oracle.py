@@ -50,7 +50,61 @@ def _load(path: Path) -> C.CDLL:
         L.ora_clamp.argtypes = [C.c_int, P(C.c_float), P(C.c_int), P(C.c_int)]
         L.ora_dp_sum.restype = C.c_int
         L.ora_dp_sum.argtypes = [P(C.c_uint32), P(C.c_uint32), C.c_int, C.c_float, P(C.c_int), P(C.c_int64)]
+        L.ora_pack.restype = C.c_int64
+        L.ora_pack.argtypes = [C.c_int, C.c_char_p, P(C.c_int64), C.c_int64, P(C.c_uint32), P(C.c_int64),
+                               P(C.c_int64)]
     return L
+
+
+def pack(db_type: int, seq, off: np.ndarray):
+    """makeDB records of raw sequences in FASTA order (the oracle's own
+    restatement of makeDB's packing): (words uint32, rec_off int64)."""
+    buf = seq.tobytes() if isinstance(seq, np.ndarray) else bytes(seq)
+    off = np.ascontiguousarray(off, dtype=np.int64)
+    n = len(off) - 1
+    nw = C.c_int64()
+    k = lib().ora_pack(db_type, buf, off.ctypes.data_as(C.POINTER(C.c_int64)), n, None, None, C.byref(nw))
+    words = np.empty(max(1, nw.value), dtype=np.uint32)
+    rec_off = np.empty(max(1, k), dtype=np.int64)
+    lib().ora_pack(db_type, buf, off.ctypes.data_as(C.POINTER(C.c_int64)), n,
+                   words.ctypes.data_as(C.POINTER(C.c_uint32)), rec_off.ctypes.data_as(C.POINTER(C.c_int64)),
+                   C.byref(nw))
+    return words[:nw.value], rec_off[:k]
+
+
+class _SynthParams(C.Structure):
+    _fields_ = [("type", C.c_int32), ("len_dist", C.c_int32), ("n_seqs", C.c_int64), ("n_ancestors", C.c_int32),
+                ("len_min", C.c_int32), ("len_max", C.c_int32), ("len_a", C.c_double), ("len_b", C.c_double),
+                ("subst_max", C.c_double), ("indel_frac", C.c_double), ("indel_max", C.c_int32),
+                ("novel_frac", C.c_double), ("seed", C.c_uint64)]
+
+
+_synth = None
+
+
+def synth(seed: int, **cfg):
+    """The seeded workload generator (oracle/_build/libsynth.so, built from
+    the generator source alone): (residues as a uint8 array, offsets[n+1])."""
+    global _synth
+    if _synth is None:
+        path = HERE / "_build" / "libsynth.so"
+        if not path.exists():
+            raise ImportError(f"{path} is missing: build it with oracle/build_oracle.py")
+        _synth = C.CDLL(str(path))
+    sp = _SynthParams(type=cfg.get("type", 0), len_dist=cfg.get("len_dist", 0), n_seqs=cfg["n_seqs"],
+                      n_ancestors=cfg["n_ancestors"], len_min=cfg["len_min"], len_max=cfg["len_max"],
+                      len_a=cfg["len_a"], len_b=cfg["len_b"], subst_max=cfg.get("subst_max", 0.2),
+                      indel_frac=cfg.get("indel_frac", 0.05), indel_max=cfg.get("indel_max", 3),
+                      novel_frac=cfg.get("novel_frac", 0.0), seed=seed)
+    sp_ptr, off_ptr, n = C.c_void_p(), C.POINTER(C.c_int64)(), C.c_int64()
+    rc = _synth.ngia_synth_generate(C.byref(sp), C.byref(sp_ptr), C.byref(off_ptr), C.byref(n))
+    if rc != 0:
+        raise RuntimeError(f"synth failed ({rc})")
+    off = np.ctypeslib.as_array(off_ptr, shape=(n.value + 1,)).copy()
+    seq = np.ctypeslib.as_array(C.cast(sp_ptr, C.POINTER(C.c_uint8)), shape=(int(off[-1]),)).copy()
+    _synth.ngia_free(sp_ptr)
+    _synth.ngia_free(C.cast(off_ptr, C.c_void_p))
+    return seq, off
 
 
 def clamp(db_type: int, s: float, w: int, precise: int = 0):

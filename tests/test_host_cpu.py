@@ -146,6 +146,41 @@ def test_db_pack_equals_makedb(tmp_path):
     assert (a.longest, a.shortest) == (b.longest, b.shortest)
 
 
+@pytest.mark.parametrize("db_type", [0, 1])
+def test_oracle_pack_and_generator_match_the_product(tmp_path, db_type):
+    """The reference arm of the benchmark builds its inputs with the oracle's
+    own makeDB packing and the generator library built on its own; both give
+    the product's bytes (edge-case FASTA included: the packer's records equal
+    the data.bin records written by makeDB)."""
+    gen = dict(type=db_type, n_seqs=300, n_ancestors=5, len_a=300.0 if db_type == 0 else 200.0,
+               len_b=90.0 if db_type == 0 else 0.6, len_dist=0 if db_type == 0 else 1, len_min=20,
+               len_max=900, subst_max=0.3, indel_max=3, seed=9)
+    seq, off = ngia.synth(**gen)
+    oseq, ooff = oracle.synth(**gen)
+    assert np.array_equal(off, ooff) and bytes(seq.seq) == oseq.tobytes()
+    a = ngia.DB.pack(db_type, seq, off)
+    w, ro = oracle.pack(db_type, oseq, ooff)
+    assert np.array_equal(a.words, w) and np.array_equal(a.rec_off, ro)
+    fa = tmp_path / "e.fasta"
+    _edge_fasta(fa, db_type, seed=11 + db_type)
+    ngia.makedb(str(fa), str(tmp_path), db_type)
+    b = ngia.DB.load(str(tmp_path))
+    recs, cur, name = [], bytearray(), None
+    for line in fa.read_bytes().split(b"\n"):
+        line = line.rstrip(b"\r")
+        if line.startswith(b">"):
+            if name is not None:
+                recs.append(bytes(cur))
+            name, cur = line, bytearray()
+        elif name is not None:
+            cur += line
+    recs.append(bytes(cur))
+    roff = np.zeros(len(recs) + 1, dtype=np.int64)
+    roff[1:] = np.cumsum([len(r) for r in recs])
+    w, ro = oracle.pack(db_type, b"".join(recs), roff)
+    assert np.array_equal(b.words, w) and np.array_equal(b.rec_off, ro)
+
+
 def test_db_load_rejects_bad_files(tmp_path):
     with pytest.raises(ngia.NgiaError) as e:
         ngia.DB.load(str(tmp_path))

@@ -31,3 +31,16 @@ def test_two_rank_replicas_report_once():
     assert len(lines) == 1, r.stdout
     out = json.loads(lines[0])
     assert out["n_gpus"] == 2 and out["value"] > 0 and out["scaling"] == "weak"
+
+
+def test_reference_arm_uses_oracle_code_only():
+    """bench.py --impl reference times the oracle on the host cores with
+    inputs built by oracle-side code: the product library is not mapped."""
+    cmd = [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "1",
+           "--n-seqs", "3000", "--workload", "dna_small"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=300, cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][-1])
+    assert out["impl"] == "reference" and out["value"] > 0
+    assert out["cpu_baseline"]["kind"] == "port" and out["cpu_baseline"]["arch"]
+    assert out["libraries"] and all(x.startswith("oracle/_build/") for x in out["libraries"]), out["libraries"]
