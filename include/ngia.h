@@ -355,15 +355,20 @@ int ngia_rep_scores_noalloc(const uint32_t *d_words, int64_t rep_off,
 int ngia_cluster_save(ngia_ctx *ctx, const char *path);
 int ngia_cluster_resume(ngia_ctx *ctx, const char *path, int32_t mode);
 
-/* Run-time tuning (no counterpart in the reference).  Three settings change
+/* Run-time tuning (no counterpart in the reference).  These settings change
  * the speed of a run, never its result: the order of the two cheap tests
  * (short-word test before or after the alignment), the number of idle lanes
- * a warp of the tiled alignment waits for before it claims new pairs, and
- * the pair count up to which a class is aligned warp-per-pair.
+ * a warp of the tiled alignment waits for before it claims new pairs, the
+ * pair count up to which a class is aligned warp-per-pair, and per length
+ * bucket (alignment class: pairs grouped by band window) its own
+ * warp-per-pair cut-off and CTA count, and the composition filter's tile.
  * ngia_autotune times candidate settings on the first `iters` greedy
  * iterations of a fresh run of this context's database (graph driver, device
  * time), keeps the fastest for later runs of the context and reports it;
- * ngia_set_tuning applies settings found before. */
+ * the result is cached in the process by database shape (type, record
+ * count and longest record, each rounded to a power of two) and parameters,
+ * and a later ngia_autotune with the same key applies it without timing
+ * (cached = 1).  ngia_set_tuning applies settings found before. */
 typedef struct ngia_tuning {
     int32_t word_order;   /* 0 by similarity, 1 short words first, 2 alignment first */
     int32_t refill;       /* 1..32 idle lanes                                        */
@@ -371,6 +376,12 @@ typedef struct ngia_tuning {
     int32_t candidates;   /* settings timed (ngia_autotune)                          */
     double  ms_per_iter;  /* device time per iteration of the chosen setting         */
     double  default_ms_per_iter;  /* the same for the default setting                */
+    int32_t class_warp_pairs[8];  /* per length bucket: its warp-per-pair cut-off,   */
+                                  /* -1 = warp_pairs                                 */
+    int32_t class_grid_div[8];    /* per length bucket: its CTAs divided by 1 or 2   */
+    int32_t filter_tile;          /* composition filter: bitmap words per warp and   */
+                                  /* tile, 8 (default) or 1                          */
+    int32_t cached;               /* 1: applied from the tuning cache, not timed     */
 } ngia_tuning;
 int ngia_autotune(ngia_ctx *ctx, const ngia_params *p, int32_t iters, ngia_tuning *out);
 int ngia_set_tuning(ngia_ctx *ctx, const ngia_tuning *t);

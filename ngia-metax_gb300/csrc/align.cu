@@ -36,6 +36,7 @@
 // moves a zero downwards within a run of ones, or adds one at the top of the
 // updated segment), so zeros_now + residues_left < cutoff is a rejection.
 // Accepted pairs are always computed to the end (their score is reported).
+#include <algorithm>
 #include <climits>
 #include <cstdlib>
 #include <mutex>
@@ -402,6 +403,12 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
     build_eq(s_pl, h.nb1, s_eq);  // the representative's match table (tile.cuh)
     __syncthreads();
   }
+  const uint32_t s_eq_s = smem_u32(s_eq);
+  // 1 and 4 as values ptxas cannot fold (nb1 is read from shared memory)
+  const uint32_t one_rt = 1u + (uint32_t)(h.nb1 < 0);
+  const FmaK fk{one_rt, one_rt << 2};
+  (void)s_eq_s;
+  (void)fk;
   typename RingOf<RING>::T ring;
   if constexpr (RING > 0) {
     ring.base = smem + (((db.max_nb * P + 3) & ~3) + kListWords) + threadIdx.x;
@@ -485,7 +492,27 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 #pragma unroll
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
     }
-    if constexpr (kEq) {
+    if constexpr (kEq && NGIA_EQ_FMA) {
+      uint32_t wc[2];
+      eq_codes_top(cur, wc);
+      uint32_t cw = 0, ncw = 0;
+      int base = js;
+      if (NGIA_EQ_NOZOLD) zw = 0;  // the tiles return their rows' zero counts
+      for (int t = 0; t < full; t++, base += MT) {
+        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, typename RingOf<RING>::T>(ring, s_eq_s, base, je, nb1, cols, wc, cw,
+                                                                           ncw, fk);
+        cw = ncw << (32 - cols);  // column 0's carry at bit 31
+        ncw = 0;
+      }
+      for (; rem >= MT; rem -= MT, base += MT) {
+        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, typename RingOf<RING>::T>(ring, s_eq_s, base, je, nb1, cols, wc, cw,
+                                                                           ncw, fk);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      if (rem > 0)
+        zw += tiled_rem_eqf<typename RingOf<RING>::T, MT>(rem, ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+    } else if constexpr (kEq) {
       rem = (rem + kEqRemRound - 1) / kEqRemRound * kEqRemRound;  // extra slots are padding
       uint32_t q[4];
       eq_codes(cur, q);
@@ -846,9 +873,12 @@ cudaError_t launch_align(ngia_ctx *c, int cls, cudaStream_t s, int score_mode) {
   DevDB db = c->db;
   RunBufs rb = c->rb;
   RunParams prm = c->prm;
-  int wp = score_mode ? -1 : c->warp_pairs;
+  // per length bucket (class): its own warp-per-pair cut-off and CTA count
+  // when the tuner chose them
+  int wp = score_mode ? -1 : (c->cls_warp_pairs[cls] >= 0 ? c->cls_warp_pairs[cls] : c->warp_pairs);
+  const int grid = std::max(1, c->grid_align[cls] / std::max(1, c->cls_grid_div[cls]));
   void *args[] = {&db, &rb, &prm, &cls, &score_mode, &wp};
-  cudaError_t e = cudaLaunchKernel((const void *)fn, dim3(c->grid_align[cls]), dim3(kAlignThreads), args,
+  cudaError_t e = cudaLaunchKernel((const void *)fn, dim3(grid), dim3(kAlignThreads), args,
                                    align_smem(c->db.type, c->db.max_nb, cls), s);
   if (e != cudaSuccess || wp <= 0) return e;  // no class can go warp-per-pair
   return cudaLaunchKernel((const void *)warp_fn(c->db.type, cls), dim3(c->grid_warp), dim3(kAlignThreads), args,

@@ -154,6 +154,7 @@ int build_graph(ngia_ctx *c) {
   }
   c->graph_exec = exec;
   c->graph_warp_pairs = c->warp_pairs;
+  c->graph_tune_gen = c->tune_gen;
   c->graph_ready = true;
   c->graph_prm = c->prm;
   return NGIA_OK;
@@ -504,7 +505,8 @@ int ngia::drv::begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, con
   rc = pull_state(c);
   if (rc) return rc;
   if (mode == NGIA_MODE_GRAPH &&
-      !(c->graph_ready && same_params(c->graph_prm, c->prm) && c->graph_warp_pairs == c->warp_pairs)) {
+      !(c->graph_ready && same_params(c->graph_prm, c->prm) && c->graph_warp_pairs == c->warp_pairs &&
+        c->graph_tune_gen == c->tune_gen)) {
     rc = build_graph(c);
     if (rc) return rc;
   }

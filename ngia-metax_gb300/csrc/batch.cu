@@ -1,13 +1,14 @@
 // batch.cu — many independent clustering jobs on one GPU.
 //
 // A batch owns one context per job (its database, run buffers and class
-// queues, grids sized to the job).  In graph form every job's whole greedy
-// loop is one launch of its CUDA graph (a conditional WHILE node re-running
-// the job's iteration — prepare, filter into length classes, align, next
-// representative — until the job is done); the batch enqueues the launches of
-// all jobs on their own streams before waiting once, so jobs run side by side
-// with no host round trip per representative anywhere in the batch.  The plain
-// form runs the jobs one after the other with the host-loop driver (the
+// queues, grids sized to the job).  In graph form the whole batch is ONE CUDA
+// graph, launched once per run: it holds one conditional WHILE node per job,
+// side by side with no edges between them, and each node's body is that
+// job's greedy iteration (prepare, filter into the length classes, align
+// every class, next representative) re-run until the job is done.  Jobs run
+// concurrently with no host round trip per representative anywhere in the
+// batch, and the graph is captured once per parameter set.  The plain form
+// runs the jobs one after the other with the host-loop driver (the
 // reference's way of working, one job per run).  Every job's result is
 // identical to clustering it alone.
 #include <algorithm>
@@ -22,15 +23,81 @@
 
 using ngia::fail;
 
-struct ngia_batch {
-  std::vector<ngia_ctx *> jobs;
-};
+
 
 #define CKB(call)                                                                                 \
   do {                                                                                            \
     cudaError_t e_ = (call);                                                                      \
     if (e_ != cudaSuccess) return fail(NGIA_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_));     \
   } while (0)
+#define CKB_(call) CKB(call)
+
+struct ngia_batch {
+  std::vector<ngia_ctx *> jobs;
+  // the batch graph: one conditional WHILE node per job
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<ngia::RunParams> prm;  // each job's parameters the graph was captured with
+  std::vector<int> warp_pairs, tune_gen;
+  cudaStream_t stream = nullptr;  // the batch graph's launch stream
+};
+
+namespace {
+
+void destroy_batch_graph(ngia_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+  b->prm.clear();
+  b->warp_pairs.clear();
+  b->tune_gen.clear();
+}
+
+bool same_prm(const ngia::RunParams &a, const ngia::RunParams &b) {
+  return a.s == b.s && a.w == b.w && a.precise == b.precise && a.word_order == b.word_order && a.refill == b.refill &&
+         a.wait_polls == b.wait_polls;
+}
+
+// Captures every job's iteration into the body of its own conditional WHILE
+// node of one graph (the job's k_next clears the node's condition when the
+// job is done or reaches its iteration limit).
+int build_batch_graph(ngia_batch *b) {
+  destroy_batch_graph(b);
+  CKB_(cudaGraphCreate(&b->graph, 0));
+  for (ngia_ctx *c : b->jobs) {
+    cudaGraphConditionalHandle cond;
+    CKB_(cudaGraphConditionalHandleCreate(&cond, b->graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    CKB_(cudaGraphAddNode(&node, b->graph, nullptr, nullptr, 0, &np));
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    CKB_(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    int rc = ngia::drv::enqueue_iteration(c, true, cond);
+    cudaGraph_t captured = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &captured);
+    if (rc != NGIA_OK || e != cudaSuccess) {
+      destroy_batch_graph(b);
+      return rc != NGIA_OK ? rc : fail(NGIA_E_CUDA, "batch graph capture: %s", cudaGetErrorString(e));
+    }
+  }
+  cudaError_t e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+  if (e != cudaSuccess) {
+    destroy_batch_graph(b);
+    return fail(NGIA_E_CUDA, "batch graph instantiate: %s", cudaGetErrorString(e));
+  }
+  for (ngia_ctx *c : b->jobs) {
+    b->prm.push_back(c->prm);
+    b->warp_pairs.push_back(c->warp_pairs);
+    b->tune_gen.push_back(c->tune_gen);
+  }
+  return NGIA_OK;
+}
+
+}  // namespace
 
 extern "C" int ngia_batch_open(const ngia_db_view *jobs, int32_t n_jobs, ngia_batch **out) {
   ngia::clear_error();
@@ -69,21 +136,33 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
       if (rc) return rc;
     }
   } else {
-    // every job's graph (built once per parameter set) is launched on the
-    // job's own stream before any of them is waited for
+    // every job is set up (run state reset, iteration limit) on its own
+    // stream; then the batch graph runs all of them in one launch
+    bool rebuild = !b->exec || b->prm.size() != nj;
     for (size_t j = 0; j < nj; j++) {
       ngia_ctx *c = b->jobs[j];
       // jobs running side by side fill the GPU: one thread per pair, the
       // form with the fewest instructions per cell (256-job batch on GB300:
       // 15.4M vs 13.0M candidate seqs/s with warp-per-pair classes)
       c->tuned_warp_pairs = 0;
-      int rc = ngia_cluster_begin(c, &params[j], NGIA_MODE_GRAPH);
+      int rc = ngia_cluster_begin(c, &params[j], NGIA_MODE_PLAIN);  // no per-job graph
       if (rc) return rc;
+      c->mode = NGIA_MODE_GRAPH;
       c->h_state->iter_limit = max_iters > 0 ? max_iters : INT64_MAX;
       CKB(cudaMemcpyAsync(&c->rb.st->iter_limit, &c->h_state->iter_limit, sizeof(int64_t),
                           cudaMemcpyHostToDevice, c->stream));
-      CKB(cudaGraphLaunch(c->graph_exec, c->stream));
+      if (!rebuild && (!same_prm(b->prm[j], c->prm) || b->warp_pairs[j] != c->warp_pairs ||
+                       b->tune_gen[j] != c->tune_gen))
+        rebuild = true;
     }
+    for (size_t j = 0; j < nj; j++) CKB(cudaStreamSynchronize(b->jobs[j]->stream));
+    if (rebuild) {
+      int rc = build_batch_graph(b);
+      if (rc) return rc;
+    }
+    if (!b->stream) CKB(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    CKB(cudaGraphLaunch(b->exec, b->stream));
+    CKB(cudaStreamSynchronize(b->stream));
   }
   ngia_stats sum;
   std::memset(&sum, 0, sizeof(sum));
@@ -112,6 +191,8 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
 
 extern "C" int ngia_batch_close(ngia_batch *b) {
   if (!b) return NGIA_OK;
+  destroy_batch_graph(b);
+  if (b->stream) cudaStreamDestroy(b->stream);
   for (ngia_ctx *c : b->jobs) ngia_close(c);
   delete b;
   return NGIA_OK;

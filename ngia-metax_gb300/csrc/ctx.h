@@ -7,6 +7,7 @@
 #include "common.cuh"
 
 struct ngia_spec;  // speculative-round driver state (spec.cu)
+static_assert(ngia::kNumClasses == 7, "per-class initialisers of ngia_ctx");
 
 struct ngia_ctx {
   int device = 0;
@@ -42,6 +43,13 @@ struct ngia_ctx {
   // test order (0 auto, 1 short words first, 2 alignment first), lockstep
   // refill threshold, warp-per-pair cut-off (-1: keep warp_pairs_default)
   int tuned_word_order = 0, tuned_refill = 32, tuned_warp_pairs = -1;
+  // per length bucket (alignment class): warp-per-pair cut-off (-1: the
+  // context's) and CTA divisor; the composition filter's words per warp
+  int cls_warp_pairs[ngia::kNumClasses] = {-1, -1, -1, -1, -1, -1, -1};
+  int cls_grid_div[ngia::kNumClasses] = {1, 1, 1, 1, 1, 1, 1};
+  int filter_tile = 8;
+  int tune_gen = 0;             // bumped by every change of the settings above
+  int graph_tune_gen = -1;      // tune_gen the captured graph was built with
   int graph_warp_pairs = -1;    // warp_pairs the captured graph was built with
   // graph form of the greedy loop
   cudaGraphExec_t graph_exec = nullptr;

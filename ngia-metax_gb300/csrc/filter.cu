@@ -427,6 +427,9 @@ __device__ __forceinline__ void flush_stats(const RunBufs &rb, unsigned long lon
 #ifndef NGIA_FILTER_WPW_WORD
 #define NGIA_FILTER_WPW_WORD 1
 #endif
+// (Issuing every header load of a warp's 8 bitmap words before the first
+// use, unpredicated per lane, made the composition-only launch slower on
+// GB300: 24.6 vs 18.1 us per iteration, 1M DNA s=0.85.)
 // NGIA_FILTER_WARP_WORD: with the short-word test in the filter, warps take
 // bitmap words independently (no tile barriers); 0 keeps the tiled loop.
 #ifndef NGIA_FILTER_WARP_WORD
@@ -800,6 +803,11 @@ cudaError_t launch_filter(ngia_ctx *c) {
         else
           k_filter_long<5><<<grid_l, 256, smem * 9, c->stream>>>(c->db, c->rb, c->prm);
       }
+    } else if (c->filter_tile == kW) {  // the tuner's choice: one bitmap word per warp and tile
+      if (P == 2)
+        k_filter<2, kW><<<grid_w, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
+      else
+        k_filter<5, kW><<<grid_w, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
     } else {
       if (P == 2)
         k_filter<2, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);

@@ -58,6 +58,28 @@
 #ifndef NGIA_EQ_REM_ROUND
 #define NGIA_EQ_REM_ROUND 1
 #endif
+//  NGIA_EQ_FMA  1: the tiled DNA kernel takes each column's code, the match
+//    words' address and the tile's carry pop/push as multiply-adds by
+//    run-time constants (IMAD on the FMA pipe, which the ALU-bound kernel
+//    leaves idle) instead of logic/shift/add instructions on the ALU pipe:
+//    +2.9% candidate seqs/s (k_align_tiled<2,64>: 7.43 -> 7.26 ms/launch).
+//  NGIA_EQ_NOZOLD  1 (with NGIA_EQ_FMA): a tile returns the zero count of
+//    its rows after the block (their sum is the window's count) instead of
+//    the change, so the rows' zero count before the block is not taken:
+//    +1.5% more (7.06 ms/launch; frac 0.688 -> 0.724 of the 3-instruction
+//    bound together).
+//  NGIA_EQ_MADC  with NGIA_EQ_FMA: every k-th slot's add-with-carry as a
+//    multiply-add with carry (IMAD.X) by a run-time 1; 0 = none (k = 2, 3
+//    ran at 0.97x, 0.98x: the core chain stays on the ALU pipe).
+#ifndef NGIA_EQ_FMA
+#define NGIA_EQ_FMA 1
+#endif
+#ifndef NGIA_EQ_MADC
+#define NGIA_EQ_MADC 0
+#endif
+#ifndef NGIA_EQ_NOZOLD
+#define NGIA_EQ_NOZOLD 1
+#endif
 
 namespace ngia {
 
@@ -261,6 +283,139 @@ __device__ __forceinline__ int tiled_tile_eq(const Ring &ring, const uint32_t *s
     }
   }
   return znew - zold;
+}
+
+// ---- match-table tiles with the per-column bookkeeping on the FMA pipe -------
+// Run-time constants 1 and 4: ptxas cannot fold a multiply by them into a
+// shift or an add, so the multiply-adds below stay IMADs (FMA pipe).
+struct FmaK {
+  uint32_t one, four;
+};
+
+// Bit i of x (i < 16) to bit 2i.
+__device__ __forceinline__ uint32_t spread16(uint32_t x) {
+  x &= 0xFFFFu;
+  x = (x | (x << 8)) & 0x00FF00FFu;
+  x = (x | (x << 4)) & 0x0F0F0F0Fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  x = (x | (x << 1)) & 0x55555555u;
+  return x;
+}
+
+// Column codes of one 32-residue query block, first column on top: w[h]
+// holds columns 16h..16h+15, two bits each (plane-1 bit above plane-0 bit),
+// column 16h in bits 31..30.
+__device__ __forceinline__ void eq_codes_top(const uint32_t (&cur)[2], uint32_t (&w)[2]) {
+  const uint32_t r0 = __brev(cur[0]), r1 = __brev(cur[1]);
+  w[0] = spread16(r0 >> 16) | (spread16(r1 >> 16) << 1);
+  w[1] = spread16(r0) | (spread16(r1) << 1);
+}
+
+// Shared-memory address of the next column's match words: code = w >> 30,
+// w <<= 2, address = eb + 4 code — three multiply-adds.
+__device__ __forceinline__ uint32_t eq_next_addr(uint32_t &w, uint32_t eb, const FmaK &k) {
+  uint32_t c, a;
+  asm("mul.hi.u32 %0, %1, %2;" : "=r"(c) : "r"(w), "r"(k.four));
+  asm("mul.lo.u32 %0, %0, %1;" : "+r"(w) : "r"(k.four));
+  asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(a) : "r"(c), "r"(k.four), "r"(eb));
+  return a;
+}
+
+// Match words of TW slots at shared address a (slot m at a + 16 m; the
+// offsets are immediates of the loads).
+template <int M, int TW>
+struct EqLoad {
+  static __device__ __forceinline__ void run(uint32_t (&e)[TW], uint32_t a) {
+    EqLoad<M - 1, TW>::run(e, a);
+    asm volatile("ld.shared.u32 %0, [%1+%2];" : "=r"(e[M - 1]) : "r"(a), "n"(16 * (M - 1)));
+  }
+};
+template <int TW>
+struct EqLoad<0, TW> {
+  static __device__ __forceinline__ void run(uint32_t (&)[TW], uint32_t) {}
+};
+template <int TW>
+__device__ __forceinline__ void eq_load_s(uint32_t (&e)[TW], uint32_t a) {
+  EqLoad<TW, TW>::run(e, a);
+}
+
+// eq_columns with the codes on top of w[] and the FMA-pipe bookkeeping.
+template <int TW, bool CC, bool PF>
+__device__ __forceinline__ void eq_columns_f(uint32_t (&row)[TW], uint32_t eb, const uint32_t (&wc)[2], int cols,
+                                             uint32_t &cw, uint32_t &ncw, const FmaK &k) {
+#pragma unroll 1
+  for (int h = 0; h < 2; h++) {
+    const int n = min(16, cols - 16 * h);
+    if (n <= 0) break;
+    uint32_t w = wc[h];
+    if constexpr (PF) {
+      uint32_t ea[TW], eo[TW];
+      eq_load_s<TW>(ea, eq_next_addr(w, eb, k));
+      int c = 0;
+#pragma unroll 1
+      for (; c + 2 <= n; c += 2) {
+        eq_load_s<TW>(eo, eq_next_addr(w, eb, k));
+        dp_tile_eqf<TW, CC, CC, NGIA_EQ_MADC>(row, ea, cw, ncw, k.one);
+        eq_load_s<TW>(ea, eq_next_addr(w, eb, k));  // past the last column: code 0, in bounds
+        dp_tile_eqf<TW, CC, CC, NGIA_EQ_MADC>(row, eo, cw, ncw, k.one);
+      }
+      if (c < n) dp_tile_eqf<TW, CC, CC, NGIA_EQ_MADC>(row, ea, cw, ncw, k.one);
+    } else {
+#pragma unroll 1
+      for (int c = 0; c < n; c++) {
+        uint32_t ev[TW];
+        eq_load_s<TW>(ev, eq_next_addr(w, eb, k));
+        dp_tile_eqf<TW, CC, CC, NGIA_EQ_MADC>(row, ev, cw, ncw, k.one);
+      }
+    }
+  }
+}
+
+// tiled_tile_eq with the FMA-pipe bookkeeping; s_eq_s is the table's
+// shared-memory address.  NGIA_EQ_NOZOLD: returns the zero count of the
+// tile's rows after the block instead of its change.
+template <int TW, bool PF, class Ring>
+__device__ __forceinline__ int tiled_tile_eqf(const Ring &ring, uint32_t s_eq_s, int base, int je, int nb1, int cols,
+                                              const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw, const FmaK &k) {
+  uint32_t row[TW];
+  int zold = 0;
+#pragma unroll
+  for (int m = 0; m < TW; m++) {
+    const int j = base + m;
+    const bool in = j <= je;
+    row[m] = in ? ring[j] : 0u;
+    if (!NGIA_EQ_NOZOLD) zold += in ? __popc(~row[m]) : 0;
+  }
+  eq_columns_f<TW, true, PF>(row, s_eq_s + 16u * (uint32_t)min(base, nb1), wc, cols, cw, ncw, k);
+  int znew = 0;
+#pragma unroll
+  for (int m = 0; m < TW; m++) {
+    const int j = base + m;
+    if (j <= je) {
+      ring[j] = row[m];
+      znew += __popc(~row[m]);
+    }
+  }
+  return znew - zold;
+}
+
+template <class Ring, int MT>
+__device__ __forceinline__ int tiled_rem_eqf(int rem, const Ring &ring, uint32_t s_eq_s, int base, int je, int nb1,
+                                             int cols, const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw,
+                                             const FmaK &k) {
+  switch (rem) {
+#define NGIA_REM(W) \
+  case W:           \
+    if (W < MT) return tiled_tile_eqf<(W < MT ? W : 1), false, Ring>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, k); \
+    return 0;
+    NGIA_REM(1) NGIA_REM(2) NGIA_REM(3) NGIA_REM(4) NGIA_REM(5) NGIA_REM(6) NGIA_REM(7) NGIA_REM(8)
+    NGIA_REM(9) NGIA_REM(10) NGIA_REM(11) NGIA_REM(12) NGIA_REM(13) NGIA_REM(14) NGIA_REM(15) NGIA_REM(16)
+    NGIA_REM(17) NGIA_REM(18) NGIA_REM(19) NGIA_REM(20) NGIA_REM(21) NGIA_REM(22) NGIA_REM(23) NGIA_REM(24)
+    NGIA_REM(25) NGIA_REM(26) NGIA_REM(27) NGIA_REM(28) NGIA_REM(29) NGIA_REM(30) NGIA_REM(31)
+#undef NGIA_REM
+    default:
+      return 0;
+  }
 }
 
 constexpr int kEqRemRound = NGIA_EQ_REM_ROUND;  // remainder tile widths: multiples of this

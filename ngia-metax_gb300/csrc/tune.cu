@@ -1,13 +1,20 @@
 // tune.cu — run-time tuning of the settings that change the speed of a run
 // but never its result: the order of the two cheap tests, the lockstep
-// refill threshold of the tiled alignment and the warp-per-pair cut-off.
-// Each candidate is timed (device time, graph driver) on the first greedy
-// iterations of a fresh run of the context's database; the fastest is kept
-// for the context's later runs.  The candidates: the default; each test
-// order; refill 24 and 28; the warp cut-off at a quarter, half and twice the
-// default.  Coordinate-wise: the best test order is kept while the refill
-// and the cut-off are tried.
+// refill threshold of the tiled alignment, the warp-per-pair cut-off, and per
+// length bucket (alignment class: the pairs of one band-window range) the
+// class's own warp-per-pair cut-off and CTA count, plus the composition
+// filter's tile.  Each candidate is timed (device time, graph driver) on the
+// first greedy iterations of a fresh run of the context's database; the
+// fastest is kept for the context's later runs.  Coordinate-wise: the
+// default; each test order; refill 24 and 28; the global cut-off at a
+// quarter, half and twice the default; then for every bucket that queued
+// pairs, thread-per-pair only, warp-per-pair up to four times the cut-off,
+// and half its CTAs; then the filter tile of one bitmap word per warp.  The
+// winner is cached in the process by database shape and parameters.
 #include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "../host/host_common.h"
@@ -17,13 +24,52 @@ using ngia::fail;
 
 namespace {
 
+constexpr int kNC = ngia::kNumClasses;
+
+struct Setting {
+  int wo = 0, rf = 32, wp = -1;
+  int cls_wp[kNC] = {-1, -1, -1, -1, -1, -1, -1};
+  int cls_div[kNC] = {1, 1, 1, 1, 1, 1, 1};
+  int ftile = 8;
+};
+
+void apply(ngia_ctx *c, const Setting &s) {
+  c->tuned_word_order = s.wo;
+  c->tuned_refill = s.rf;
+  c->tuned_warp_pairs = s.wp;
+  for (int k = 0; k < kNC; k++) {
+    c->cls_warp_pairs[k] = s.cls_wp[k];
+    c->cls_grid_div[k] = s.cls_div[k];
+  }
+  c->filter_tile = s.ftile;
+  c->tune_gen++;
+}
+
+// Cache key: type, log2 of record count and of the longest record (in plane
+// blocks), the parameters and the iterations timed.
+using Key = std::tuple<int, int, int, uint32_t, int, int, int>;
+std::mutex g_cache_mu;
+std::map<Key, std::pair<Setting, double>> g_cache;
+
+int log2_ceil(int64_t x) {
+  int k = 0;
+  while ((int64_t(1) << k) < x) k++;
+  return k;
+}
+
+Key key_of(const ngia_ctx *c, const ngia_params *p, int iters) {
+  uint32_t sb;
+  std::memcpy(&sb, &p->similarity, 4);
+  return Key(c->db.type, log2_ceil(c->db.n), log2_ceil(c->db.max_nb), sb, p->word_length * 2 + p->precise, iters,
+             c->batch_member ? 1 : 0);
+}
+
 // Device time per iteration of `iters` fresh iterations with these settings
-// (one untimed run first: graph capture and warm caches).
-int time_setting(ngia_ctx *c, const ngia_params *p, int32_t iters, int word_order, int refill, int warp_pairs,
-                 double *ms_per_iter) {
-  c->tuned_word_order = word_order;
-  c->tuned_refill = refill;
-  c->tuned_warp_pairs = warp_pairs;
+// (one untimed run first: graph capture and warm caches); pairs[] receives
+// the pairs each class queued.
+int time_setting(ngia_ctx *c, const ngia_params *p, int32_t iters, const Setting &s, double *ms_per_iter,
+                 int64_t *pairs) {
+  apply(c, s);
   float total = 0.f;
   int64_t done_iters = 0;
   for (int rep = 0; rep < 2; rep++) {
@@ -36,10 +82,28 @@ int time_setting(ngia_ctx *c, const ngia_params *p, int32_t iters, int word_orde
       rc = ngia_step_device_ms(c, &total);
       if (rc) return rc;
       done_iters = c->h_state->iter;
+      for (int k = 0; k < kNC; k++) pairs[k] = (int64_t)c->h_state->st_class_pairs[k];
     }
   }
   *ms_per_iter = done_iters > 0 ? total / (double)done_iters : 0.0;
   return NGIA_OK;
+}
+
+void report(const Setting &s, int count, double best, double base, int cached, ngia_tuning *out) {
+  if (!out) return;
+  std::memset(out, 0, sizeof(*out));
+  out->word_order = s.wo;
+  out->refill = s.rf;
+  out->warp_pairs = s.wp;
+  out->candidates = count;
+  out->ms_per_iter = best;
+  out->default_ms_per_iter = base;
+  for (int k = 0; k < 8; k++) {
+    out->class_warp_pairs[k] = k < kNC ? s.cls_wp[k] : -1;
+    out->class_grid_div[k] = k < kNC ? s.cls_div[k] : 1;
+  }
+  out->filter_tile = s.ftile;
+  out->cached = cached;
 }
 
 }  // namespace
@@ -49,62 +113,112 @@ extern "C" int ngia_autotune(ngia_ctx *c, const ngia_params *p, int32_t iters, n
   if (!c || !p || iters <= 0) return fail(NGIA_E_ARG, "ngia_autotune: bad argument");
   int rc = ngia::drv::validate_params(c->db.type, p);
   if (rc) return rc;
+  const Key key = key_of(c, p, iters);
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    auto it = g_cache.find(key);
+    if (it != g_cache.end()) {
+      const Setting s = it->second.first;
+      apply(c, s);
+      c->warp_pairs = s.wp >= 0 ? s.wp : c->warp_pairs_default;
+      c->begun = false;
+      report(s, 0, it->second.second, 0.0, 1, out);
+      return NGIA_OK;
+    }
+  }
   const int def_wp = c->warp_pairs_default;
-  int best_wo = 0, best_rf = 32, best_wp = -1, count = 0;
+  Setting best_s;
+  int count = 0;
   double best = 0.0, base = 0.0;
-  auto trial = [&](int wo, int rf, int wp) -> int {
+  int64_t pairs[kNC] = {0};
+  auto trial = [&](const Setting &s) -> int {
     double ms = 0.0;
-    const int r = time_setting(c, p, iters, wo, rf, wp, &ms);
+    int64_t pr[kNC];
+    const int r = time_setting(c, p, iters, s, &ms, pr);
     if (r) return r;
     count++;
-    if (count == 1) base = ms;
+    if (count == 1) {
+      base = ms;
+      for (int k = 0; k < kNC; k++) pairs[k] = pr[k];
+    }
     if (count == 1 || ms < best) {
       best = ms;
-      best_wo = wo;
-      best_rf = rf;
-      best_wp = wp;
+      best_s = s;
     }
     return NGIA_OK;
   };
-  rc = trial(0, 32, -1);  // the default
-  for (int wo : {1, 2})
-    if (!rc && !(c->db.has_short && !p->precise && wo == 2)) rc = trial(wo, 32, -1);  // short records: word first
-  const int wo = best_wo;
-  for (int rf : {24, 28})
-    if (!rc) rc = trial(wo, rf, best_wp);
-  const int rf = best_rf;
-  for (int wp : {def_wp / 4, def_wp / 2, def_wp * 2})
-    if (!rc) rc = trial(wo, rf, wp);
+  rc = trial(Setting());  // the default
+  for (int wo : {1, 2}) {
+    if (rc || (c->db.has_short && !p->precise && wo == 2)) continue;  // short records: word first
+    Setting s;
+    s.wo = wo;
+    rc = trial(s);
+  }
+  for (int rf : {24, 28}) {
+    if (rc) break;
+    Setting s = best_s;
+    s.rf = rf;
+    rc = trial(s);
+  }
+  for (int wp : {def_wp / 4, def_wp / 2, def_wp * 2}) {
+    if (rc) break;
+    Setting s = best_s;
+    s.wp = wp;
+    rc = trial(s);
+  }
+  // per length bucket: the classes that queued pairs in the default run
+  const int cut = best_s.wp >= 0 ? best_s.wp : def_wp;
+  for (int k = 0; k < ngia::num_classes(c->db.type) && !rc; k++) {
+    if (!pairs[k]) continue;
+    for (int v = 0; v < 3 && !rc; v++) {
+      Setting s = best_s;
+      if (v == 0) s.cls_wp[k] = 0;        // thread per pair only
+      if (v == 1) s.cls_wp[k] = 4 * cut;  // warp per pair up to 4x the cut-off
+      if (v == 2) s.cls_div[k] = 2;       // half the CTAs
+      if (v == 1 && cut <= 0) continue;
+      rc = trial(s);
+    }
+  }
+  if (!rc) {
+    Setting s = best_s;
+    s.ftile = 1;
+    rc = trial(s);
+  }
   if (rc) {
-    c->tuned_word_order = 0;
-    c->tuned_refill = 32;
-    c->tuned_warp_pairs = -1;
+    apply(c, Setting());
+    c->warp_pairs = def_wp;
     return rc;
   }
-  c->tuned_word_order = best_wo;
-  c->tuned_refill = best_rf;
-  c->tuned_warp_pairs = best_wp;
-  c->warp_pairs = best_wp >= 0 ? best_wp : def_wp;
+  apply(c, best_s);
+  c->warp_pairs = best_s.wp >= 0 ? best_s.wp : def_wp;
   c->begun = false;
-  if (out) {
-    out->word_order = best_wo;
-    out->refill = best_rf;
-    out->warp_pairs = best_wp;
-    out->candidates = count;
-    out->ms_per_iter = best;
-    out->default_ms_per_iter = base;
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    g_cache[key] = {best_s, best};
   }
+  report(best_s, count, best, base, 0, out);
   return NGIA_OK;
 }
 
 extern "C" int ngia_set_tuning(ngia_ctx *c, const ngia_tuning *t) {
   ngia::clear_error();
   if (!c || !t) return fail(NGIA_E_ARG, "ngia_set_tuning: null argument");
-  if (t->word_order < 0 || t->word_order > 2 || t->refill < 1 || t->refill > 32 || t->warp_pairs < -1)
+  if (t->word_order < 0 || t->word_order > 2 || t->refill < 1 || t->refill > 32 || t->warp_pairs < -1 ||
+      (t->filter_tile != 8 && t->filter_tile != 1 && t->filter_tile != 0))
     return fail(NGIA_E_ARG, "ngia_set_tuning: setting out of range");
-  c->tuned_word_order = t->word_order;
-  c->tuned_refill = t->refill;
-  c->tuned_warp_pairs = t->warp_pairs;
+  Setting s;
+  s.wo = t->word_order;
+  s.rf = t->refill;
+  s.wp = t->warp_pairs;
+  for (int k = 0; k < kNC; k++) {
+    if (t->class_warp_pairs[k] < -1 || (t->class_grid_div[k] != 0 && t->class_grid_div[k] != 1 &&
+                                        t->class_grid_div[k] != 2))
+      return fail(NGIA_E_ARG, "ngia_set_tuning: per-class setting out of range");
+    s.cls_wp[k] = t->class_warp_pairs[k];
+    s.cls_div[k] = t->class_grid_div[k] ? t->class_grid_div[k] : 1;
+  }
+  s.ftile = t->filter_tile ? t->filter_tile : 8;
+  apply(c, s);
   c->warp_pairs = t->warp_pairs >= 0 ? t->warp_pairs : c->warp_pairs_default;
   return NGIA_OK;
 }

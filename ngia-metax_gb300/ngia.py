@@ -60,7 +60,9 @@ class ServeResult(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("word_order", C.c_int32), ("refill", C.c_int32), ("warp_pairs", C.c_int32),
-                ("candidates", C.c_int32), ("ms_per_iter", C.c_double), ("default_ms_per_iter", C.c_double)]
+                ("candidates", C.c_int32), ("ms_per_iter", C.c_double), ("default_ms_per_iter", C.c_double),
+                ("class_warp_pairs", C.c_int32 * 8), ("class_grid_div", C.c_int32 * 8), ("filter_tile", C.c_int32),
+                ("cached", C.c_int32)]
 
 
 class Stats(C.Structure):
@@ -483,10 +485,15 @@ class Context:
         """Times the speed-only settings on the first iterations; keeps the fastest."""
         t = Tuning()
         _check(lib().ngia_autotune(self._h, C.byref(params), iters, C.byref(t)))
-        return {f: getattr(t, f) for f, _ in Tuning._fields_}
+        return {f: (list(getattr(t, f)) if f.startswith("class_") else getattr(t, f)) for f, _ in Tuning._fields_}
 
-    def set_tuning(self, word_order: int = 0, refill: int = 32, warp_pairs: int = -1) -> None:
+    def set_tuning(self, word_order: int = 0, refill: int = 32, warp_pairs: int = -1, class_warp_pairs=None,
+                   class_grid_div=None, filter_tile: int = 8) -> None:
         t = Tuning(word_order, refill, warp_pairs, 0, 0.0, 0.0)
+        for k in range(8):
+            t.class_warp_pairs[k] = -1 if class_warp_pairs is None else class_warp_pairs[k]
+            t.class_grid_div[k] = 1 if class_grid_div is None else class_grid_div[k]
+        t.filter_tile = filter_tile
         _check(lib().ngia_set_tuning(self._h, C.byref(t)))
 
     def save(self, path: str) -> None:

@@ -228,8 +228,23 @@ def test_tuning_changes_speed_not_results(cuda_device, db_type, s, w):
             ctx.set_tuning(wo, rf, wp)
             got.append(ctx.cluster(p, ngia.MODE_GRAPH))
             got.append(ctx.cluster(p, ngia.MODE_PLAIN))
+        # per length bucket: alternating thread-only / warp-heavy cut-offs and
+        # halved CTA counts, and the one-word filter tile
+        ctx.set_tuning(2 if db_type == 0 else 1, 32, -1, class_warp_pairs=[0, 10 ** 6] * 4,
+                       class_grid_div=[2, 1] * 4, filter_tile=1)
+        got.append(ctx.cluster(p, ngia.MODE_GRAPH))
+        got.append(ctx.cluster(p, ngia.MODE_PLAIN))
         with pytest.raises(ngia.NgiaError):
             ctx.set_tuning(3, 32, -1)
+        with pytest.raises(ngia.NgiaError):
+            ctx.set_tuning(0, 32, -1, filter_tile=4)
+    with ngia.Context(db) as ctx:  # the same database shape and parameters: from the cache
+        t2 = ctx.autotune(p, iters=3)
+        assert t2["cached"] == 1 and t2["candidates"] == 0
+        assert (t2["word_order"], t2["refill"], t2["warp_pairs"], t2["filter_tile"]) == \
+            (t["word_order"], t["refill"], t["warp_pairs"], t["filter_tile"])
+        assert t2["class_warp_pairs"] == t["class_warp_pairs"] and t2["class_grid_div"] == t["class_grid_div"]
+        got.append(ctx.cluster(p, ngia.MODE_GRAPH))
     for cl, ident, _ in got:
         assert np.array_equal(cl, ocl) and np.array_equal(ident, oid)
 
