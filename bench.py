@@ -252,15 +252,18 @@ def run_reference(args, dist: Dist):
 
 
 # ---- our arm ------------------------------------------------------------------------
-def stage_replay(ctx, ck: str, iters: int) -> dict:
+def stage_replay(ctx, ck: str, iters: int, floor: bool = False) -> dict:
     """Resumes the checkpoint taken at the start of the timed region in the
     plain driver with CUDA events around every stage launch on the library
     stream and runs the same `iters` greedy iterations again; returns the
     stage times and the work counters of exactly those iterations, and the
-    assignment they end with."""
+    assignment they end with.  `floor`: first measures the composition
+    filter's floor (empty launch, read-only pass) on the unclustered set the
+    timed region starts from."""
     import ngia
 
     ctx.resume(ck, ngia.MODE_PLAIN)
+    fl = ctx.filter_floor() if floor else None
     a = ctx.stats()
     ctx.set_profiling(True)
     ctx.step(iters)
@@ -272,6 +275,7 @@ def stage_replay(ctx, ck: str, iters: int) -> dict:
     for k in ("class_pairs", "class_cells", "class_bytes"):
         d[k] = [y - x for x, y in zip(a[k], b[k])]
     d["class_ms"] = list(b["class_ms"])
+    d["floor_us"] = fl
     return d, cl, ident
 
 
@@ -312,10 +316,20 @@ def filter_roofline(rep: dict, peaks: dict) -> dict:
     it = max(1, rep["iterations"])
     ms = rep["ms_filter"]
     gbs = rep["filter_bytes"] / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
-    return {"bound": "hbm", "kernel": "k_prep + k_filter", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-            "frac": gbs / peaks["hbm_gbs"], "traffic": rep["filter_bytes"] / it, "peak_source": peaks["source"],
-            "traffic_kind": "algorithmic filter bytes per iteration (headers of every candidate, planes of the "
-                            "word-tested ones)", "ms_filter_per_iter": ms / it}
+    out = {"bound": "hbm", "kernel": "k_prep + k_filter", "achieved": gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+           "frac": gbs / peaks["hbm_gbs"], "traffic": rep["filter_bytes"] / it, "peak_source": peaks["source"],
+           "traffic_kind": "algorithmic filter bytes per iteration (headers of every candidate, planes of the "
+                           "word-tested ones)", "ms_filter_per_iter": ms / it}
+    if rep.get("floor_us"):
+        launch_us, read_us = rep["floor_us"]
+        # at the start of the timed region: the unclustered set is largest there
+        out["floor"] = {"empty_launch_us": launch_us, "read_only_us": read_us,
+                        "hbm_time_us": 1e6 * (rep["filter_bytes"] / it) / (peaks["hbm_gbs"] * 1e9),
+                        "filter_us": 1e3 * ms / it, "filter_over_read_only": (1e3 * ms / it) / read_us if read_us else None,
+                        "how": "same grid as the composition filter, same stream, 20 launches each, on the unclustered "
+                               "set the timed region starts from: an empty kernel, and one that only reads each "
+                               "warp's bitmap words and then the length and counts of every unclustered sequence"}
+    return out
 
 
 def timed_run(args, dist, db, cfg, p, S: int, steps: int, warmup: int, autotune: int, clocks: bool = True):
@@ -349,7 +363,7 @@ def timed_run(args, dist, db, cfg, p, S: int, steps: int, warmup: int, autotune:
         st1 = ctx.stats()
         dist.barrier()
         cl_t, id_t, _ = ctx.end()
-        rep, cl_r, id_r = stage_replay(ctx, ck, S * steps)
+        rep, cl_r, id_r = stage_replay(ctx, ck, S * steps, floor=cfg["type"] == 0)
     ctx.close()
     return {"tuning": tuning, "dev_ms": dev_ms, "t_wall": t_wall, "clocks": clk_out,
             "cands": st1["candidates"] - st0["candidates"], "cells": st1["band_cells"] - st0["band_cells"],

@@ -324,6 +324,15 @@ int ngia_unpin_host(void *ptr);
  * alignment inner loop); *gops receives lane-operations per second / 1e9. */
 int ngia_measure_int_peak(double *gops);
 
+/* The floor under the composition filter's time on an open, begun DNA
+ * context: *launch_us = the mean device time of an empty kernel launched
+ * with the filter's grid, *read_us = the mean time of a kernel with the same
+ * grid that only reads what the filter reads for the current unclustered set
+ * (each warp's bitmap words, then length and counts of every unclustered
+ * sequence in them).  The run state is not changed.  No reference
+ * counterpart: it bounds kernel_baseFilterGen (func.cu:323-338) from below. */
+int ngia_measure_filter_floor(ngia_ctx *ctx, double *launch_us, double *read_us);
+
 /* Banded-LCS scores of the representative record at d_words + rep_off
  * against the n query records at d_words + d_query_off[k], written to
  * d_scores[k]; all three arrays are device memory the caller owns, and the

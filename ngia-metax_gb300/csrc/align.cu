@@ -485,6 +485,11 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
     constexpr int MT = tiled_main(P);
     const int full = (int)__reduce_min_sync(kFullMask, busy ? (unsigned)(n / MT) : 0xFFFFFFFFu);
     int rem = (int)__reduce_max_sync(kFullMask, busy ? (unsigned)(n - MT * full) : 0u);
+    // every busy lane's window ends exactly at the warp's last tile slot
+    // (all lanes vote, before the idle ones leave the body)
+    bool exact_cover = false;
+    if constexpr (kEq && NGIA_EQ_FMA && NGIA_EQ_ZCARRY) exact_cover = __all_sync(kFullMask, !busy || n - MT * full == rem);
+    (void)exact_cover;
     if (!busy) continue;
     const int cols = (i == nq - 1) ? lastcols : 32;
     n_done += (unsigned long long)n * cols;
@@ -493,25 +498,38 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
     }
     if constexpr (kEq && NGIA_EQ_FMA) {
+      using Ring = typename RingOf<RING>::T;
+      constexpr bool kZC = !NGIA_EQ_ZCARRY;  // tiles count zeros
       uint32_t wc[2];
       eq_codes_top(cur, wc);
-      uint32_t cw = 0, ncw = 0;
+      uint32_t cw = 0, ncw = 0, last = 0;
       int base = js;
-      if (NGIA_EQ_NOZOLD) zw = 0;  // the tiles return their rows' zero counts
+      if (kZC && NGIA_EQ_NOZOLD) zw = 0;  // the tiles return their rows' zero counts
       for (int t = 0; t < full; t++, base += MT) {
-        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, typename RingOf<RING>::T>(ring, s_eq_s, base, je, nb1, cols, wc, cw,
-                                                                           ncw, fk);
+        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+        last = ncw;
         cw = ncw << (32 - cols);  // column 0's carry at bit 31
         ncw = 0;
       }
       for (; rem >= MT; rem -= MT, base += MT) {
-        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, typename RingOf<RING>::T>(ring, s_eq_s, base, je, nb1, cols, wc, cw,
-                                                                           ncw, fk);
+        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+        last = ncw;
         cw = ncw << (32 - cols);
         ncw = 0;
       }
-      if (rem > 0)
-        zw += tiled_rem_eqf<typename RingOf<RING>::T, MT>(rem, ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+      if (rem > 0) {
+        zw += tiled_rem_eqf<Ring, MT, kZC>(rem, ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+        last = ncw;
+      }
+      if constexpr (!kZC) {
+        if (exact_cover) {
+          zw += __popc(last);  // the carries out of the window's top row over the block's columns
+        } else {
+          int z = 0;
+          for (int j = js; j <= je; j++) z += __popc(~ring[j]);
+          zw = z;
+        }
+      }
     } else if constexpr (kEq) {
       rem = (rem + kEqRemRound - 1) / kEqRemRound * kEqRemRound;  // extra slots are padding
       uint32_t q[4];

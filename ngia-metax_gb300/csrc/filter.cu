@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <climits>
 
+#include "../host/host_common.h"
 #include "ctx.h"
 #include "kmer.cuh"
 
@@ -976,3 +977,84 @@ cudaError_t launch_score_classify(ngia_ctx *c, int n) {
 }
 
 }  // namespace ngia
+
+namespace ngia {
+// ---- the floor under the composition filter's time ---------------------------
+// Two kernels with the composition filter's grid and tiles: one that does
+// nothing, and one that only reads what the filter reads (each warp's bitmap
+// words, then the length and counts of every unclustered sequence of them),
+// folding the values so the loads are kept.  Their times on the context's
+// stream bound the filter's: launch and one round of dependent loads.
+namespace {
+
+__global__ void k_floor_empty(const RunBufs rb) {
+  if (threadIdx.x == 0 && blockIdx.x == 0 && rb.st == nullptr) rb.fstats[0] = 1;
+}
+
+__global__ void __launch_bounds__(256) k_floor_read(DevDB db, RunBufs rb, unsigned long long *sink) {
+  constexpr int kW = NGIA_FILTER_WPW_BASE, kTileWords = 8 * kW;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nbw = (db.n + 31) / 32;
+  const int tiles = (nbw + kTileWords - 1) / kTileWords;
+  uint32_t acc = 0;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    uint32_t bits_of[kW];
+#pragma unroll
+    for (int k = 0; k < kW; k++) {
+      const int wi = tile * kTileWords + warp * kW + k;
+      bits_of[k] = wi < nbw ? rb.alive[wi] : 0u;
+    }
+#pragma unroll
+    for (int k = 0; k < kW; k++) {
+      const int c = (tile * kTileWords + warp * kW + k) * 32 + lane;
+      if ((bits_of[k] >> lane) & 1u) {
+        const uint4 q = __ldg(reinterpret_cast<const uint4 *>(db.cnt) + c);
+        acc += (uint32_t)__ldg(db.len + c) + q.x + q.y + q.z + q.w;
+      }
+    }
+  }
+  // A thread sums at most 8 x 5 values below 2^16 (< 2^22), so this never
+  // holds; the compiler cannot know that and keeps the loads.
+  if (acc == 0xFFFFFFFFu) atomicAdd(sink, 1ull);
+}
+
+}  // namespace
+}  // namespace ngia
+
+extern "C" int ngia_measure_filter_floor(ngia_ctx *c, double *launch_us, double *read_us) {
+  ngia::clear_error();
+  if (!c || !launch_us || !read_us) return ngia::fail(NGIA_E_ARG, "ngia_measure_filter_floor: null argument");
+  if (!c->begun) return ngia::fail(NGIA_E_STATE, "ngia_measure_filter_floor before ngia_cluster_begin");
+  if (c->db.type != 0) return ngia::fail(NGIA_E_ARG, "ngia_measure_filter_floor: DNA databases only");
+  const int nbw = (c->db.n + 31) / 32;
+  constexpr int kB = NGIA_FILTER_WPW_BASE;
+  const int grid = std::max(1, std::min(c->grid_filter, (nbw + 8 * kB - 1) / (8 * kB)));
+  constexpr int kReps = 20;
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e == cudaSuccess) e = cudaEventCreate(&e2);
+  // the sink (written only in the impossible case above): the last counter
+  // of the filter-statistics stripes
+  unsigned long long *sink = c->rb.fstats + ngia::kFilterStripes * ngia::kFilterStats - 1;
+  if (e == cudaSuccess) {
+    ngia::k_floor_empty<<<grid, 256, 0, c->stream>>>(c->rb);  // warm-up
+    ngia::k_floor_read<<<grid, 256, 0, c->stream>>>(c->db, c->rb, sink);
+    cudaEventRecord(e0, c->stream);
+    for (int r = 0; r < kReps; r++) ngia::k_floor_empty<<<grid, 256, 0, c->stream>>>(c->rb);
+    cudaEventRecord(e1, c->stream);
+    for (int r = 0; r < kReps; r++) ngia::k_floor_read<<<grid, 256, 0, c->stream>>>(c->db, c->rb, sink);
+    cudaEventRecord(e2, c->stream);
+    e = cudaEventSynchronize(e2);
+  }
+  float a = 0.f, b = 0.f;
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&a, e0, e1);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(&b, e1, e2);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e2) cudaEventDestroy(e2);
+  if (e != cudaSuccess) return ngia::fail(NGIA_E_CUDA, "ngia_measure_filter_floor: %s", cudaGetErrorString(e));
+  *launch_us = 1e3 * a / kReps;
+  *read_us = 1e3 * b / kReps;
+  return NGIA_OK;
+}

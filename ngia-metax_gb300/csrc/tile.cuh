@@ -80,6 +80,16 @@
 #ifndef NGIA_EQ_NOZOLD
 #define NGIA_EQ_NOZOLD 1
 #endif
+//  NGIA_EQ_ZCARRY  1 (with NGIA_EQ_FMA): the tiles count no zeros at all.
+//    Over one column a window's zero count grows by exactly the carry out of
+//    its top row (with carry 0 into its bottom; checked exhaustively on
+//    small widths), so when every busy lane of the warp fills the warp's
+//    tiles exactly (no padding slot above its window) the block's growth is
+//    the popcount of the last tile's carry-out word; otherwise the window is
+//    recounted from the ring.
+#ifndef NGIA_EQ_ZCARRY
+#define NGIA_EQ_ZCARRY 0
+#endif
 
 namespace ngia {
 
@@ -374,7 +384,7 @@ __device__ __forceinline__ void eq_columns_f(uint32_t (&row)[TW], uint32_t eb, c
 // tiled_tile_eq with the FMA-pipe bookkeeping; s_eq_s is the table's
 // shared-memory address.  NGIA_EQ_NOZOLD: returns the zero count of the
 // tile's rows after the block instead of its change.
-template <int TW, bool PF, class Ring>
+template <int TW, bool PF, class Ring, bool ZC = true>
 __device__ __forceinline__ int tiled_tile_eqf(const Ring &ring, uint32_t s_eq_s, int base, int je, int nb1, int cols,
                                               const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw, const FmaK &k) {
   uint32_t row[TW];
@@ -384,7 +394,7 @@ __device__ __forceinline__ int tiled_tile_eqf(const Ring &ring, uint32_t s_eq_s,
     const int j = base + m;
     const bool in = j <= je;
     row[m] = in ? ring[j] : 0u;
-    if (!NGIA_EQ_NOZOLD) zold += in ? __popc(~row[m]) : 0;
+    if (ZC && !NGIA_EQ_NOZOLD) zold += in ? __popc(~row[m]) : 0;
   }
   eq_columns_f<TW, true, PF>(row, s_eq_s + 16u * (uint32_t)min(base, nb1), wc, cols, cw, ncw, k);
   int znew = 0;
@@ -393,20 +403,20 @@ __device__ __forceinline__ int tiled_tile_eqf(const Ring &ring, uint32_t s_eq_s,
     const int j = base + m;
     if (j <= je) {
       ring[j] = row[m];
-      znew += __popc(~row[m]);
+      if (ZC) znew += __popc(~row[m]);
     }
   }
   return znew - zold;
 }
 
-template <class Ring, int MT>
+template <class Ring, int MT, bool ZC = true>
 __device__ __forceinline__ int tiled_rem_eqf(int rem, const Ring &ring, uint32_t s_eq_s, int base, int je, int nb1,
                                              int cols, const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw,
                                              const FmaK &k) {
   switch (rem) {
 #define NGIA_REM(W) \
   case W:           \
-    if (W < MT) return tiled_tile_eqf<(W < MT ? W : 1), false, Ring>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, k); \
+    if (W < MT) return tiled_tile_eqf<(W < MT ? W : 1), false, Ring, ZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, k); \
     return 0;
     NGIA_REM(1) NGIA_REM(2) NGIA_REM(3) NGIA_REM(4) NGIA_REM(5) NGIA_REM(6) NGIA_REM(7) NGIA_REM(8)
     NGIA_REM(9) NGIA_REM(10) NGIA_REM(11) NGIA_REM(12) NGIA_REM(13) NGIA_REM(14) NGIA_REM(15) NGIA_REM(16)

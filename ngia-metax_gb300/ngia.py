@@ -116,6 +116,7 @@ def lib() -> C.CDLL:
         "ngia_pin_host": (C.c_int, [VP, C.c_size_t]),
         "ngia_unpin_host": (C.c_int, [VP]),
         "ngia_measure_int_peak": (C.c_int, [P(C.c_double)]),
+        "ngia_measure_filter_floor": (C.c_int, [VP, P(C.c_double), P(C.c_double)]),
         "ngia_cluster_stats": (C.c_int, [VP, P(Stats)]),
         "ngia_step_device_ms": (C.c_int, [VP, P(C.c_float)]),
         "ngia_set_profiling": (C.c_int, [VP, I32]),
@@ -532,6 +533,13 @@ class Context:
 
     def set_profiling(self, on: bool) -> None:
         _check(lib().ngia_set_profiling(self._h, 1 if on else 0))
+
+    def filter_floor(self) -> tuple[float, float]:
+        """(empty launch, read-only pass) in microseconds on the filter's grid
+        for the current unclustered set (DNA, begun context)."""
+        a, b = C.c_double(), C.c_double()
+        _check(lib().ngia_measure_filter_floor(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def pair_scores(self, params: Params, rep: int, cands) -> np.ndarray:
         c = np.ascontiguousarray(cands, dtype=np.int32)
