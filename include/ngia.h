@@ -213,12 +213,27 @@ typedef struct ngia_batch ngia_batch;
  * copied to the device with grids sized to the job). */
 int ngia_batch_open(const ngia_db_view *jobs, int32_t n_jobs, ngia_batch **out);
 
+/* Batch-only driver form: the jobs of one record type advance together, one
+ * representative each per round, and every stage of a round is one launch
+ * over all of them (cross-job work queues per length bucket). */
+#define NGIA_MODE_POOL   3
+
 /* Clusters every job with its own parameters (params[j], clamped).
- * NGIA_MODE_GRAPH: every job's whole greedy loop is one launch of its CUDA
- * graph (a conditional while node); all launches are queued, each on the
- * job's own stream, before the batch waits once, so jobs run side by side
- * with no host round trip per representative;
+ * NGIA_MODE_GRAPH: the whole batch is one launch of one CUDA graph holding
+ * one conditional while node per job, side by side, so jobs run
+ * concurrently with no host round trip per representative;
+ * NGIA_MODE_POOL: one launch of one CUDA graph holding one while node per
+ * record type: each round prepares every job's representative, filters the
+ * unclustered sequences of all jobs in one launch into each job's length
+ * buckets (alignment classes), and aligns each bucket across all jobs in one
+ * persistent launch whose CTAs claim chunks of pairs from any job and stage
+ * that job's representative in shared memory.  A job whose database has
+ * records of net length < 16 while precise is 0 keeps its own while node
+ * (the reference's word kernel then depends on job positions, func.cu:375);
+ * at most 8,192 jobs of one record type (NGIA_E_LIMIT beyond);
  * NGIA_MODE_PLAIN: the jobs one after the other with the host-loop driver.
+ * No reference counterpart (the reference clusters one database per run,
+ * cluster.cpp:4-17).
  * max_iters > 0 stops each job after that many representatives (sampling).
  * cluster_out[j] / identity_out[j] (either may be NULL) receive job j's
  * arrays (jobs[j].n entries); stats (may be NULL) the sums over jobs.

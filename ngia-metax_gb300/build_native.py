@@ -25,7 +25,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
 CXX = os.environ.get("CXX", "g++")
 
-CU_SOURCES = ["csrc/filter.cu", "csrc/align.cu", "csrc/api.cu", "csrc/probe.cu", "csrc/noalloc.cu", "csrc/batch.cu", "csrc/serve.cu", "csrc/checkpoint.cu", "csrc/tune.cu", "csrc/spec.cu"]
+CU_SOURCES = ["csrc/filter.cu", "csrc/align.cu", "csrc/api.cu", "csrc/probe.cu", "csrc/noalloc.cu", "csrc/batch.cu", "csrc/serve.cu", "csrc/checkpoint.cu", "csrc/tune.cu", "csrc/spec.cu", "csrc/pool.cu"]
 CPP_SOURCES = ["host/errors.cpp", "host/synth.cpp", "host/dbformat.cpp"]
 TOOLS = {"cluster": "host/cluster_main.cpp", "makeDB": "host/makedb_main.cpp", "ngia_synth": "host/synth_main.cpp"}
 

@@ -40,6 +40,15 @@ struct ngia_batch {
   std::vector<ngia::RunParams> prm;  // each job's parameters the graph was captured with
   std::vector<int> warp_pairs, tune_gen;
   cudaStream_t stream = nullptr;  // the batch graph's launch stream
+  // the pooled form: one pool per record type, and its graph (one WHILE node
+  // per pool plus one per job the pools do not take)
+  ngia::pool::Group *pool[2] = {nullptr, nullptr};
+  cudaGraph_t pgraph = nullptr;
+  cudaGraphExec_t pexec = nullptr;
+  std::vector<int> pooled;                // per job: 1 in its type's pool, 0 own node
+  std::vector<ngia::RunParams> pprm;      // parameters of the own-node jobs at capture
+  std::vector<int> ptune;                 // their tuning generation at capture
+  cudaStream_t pstream = nullptr;         // capture and launch stream of the pooled graph
 };
 
 namespace {
@@ -97,6 +106,100 @@ int build_batch_graph(ngia_batch *b) {
   return NGIA_OK;
 }
 
+void destroy_pool_graph(ngia_batch *b) {
+  if (b->pexec) cudaGraphExecDestroy(b->pexec);
+  if (b->pgraph) cudaGraphDestroy(b->pgraph);
+  b->pexec = nullptr;
+  b->pgraph = nullptr;
+  for (auto &g : b->pool) {
+    ngia::pool::group_close(g);
+    g = nullptr;
+  }
+  b->pooled.clear();
+  b->pprm.clear();
+  b->ptune.clear();
+}
+
+// A job the pools can take: its greedy loop needs no per-job exact
+// short-word path (no record of net length < 16 while the test is on).
+bool poolable(const ngia_ctx *c) { return !(c->db.has_short && !c->prm.precise); }
+
+// The pooled graph: one WHILE node per non-empty pool (its body is one round
+// of the pool) and one per job outside the pools (its own iteration).
+int build_pool_graph(ngia_batch *b) {
+  destroy_pool_graph(b);
+  std::vector<ngia_ctx *> members[2];
+  for (ngia_ctx *c : b->jobs) {
+    b->pooled.push_back(poolable(c) ? 1 : 0);
+    b->pprm.push_back(c->prm);
+    b->ptune.push_back(c->tune_gen);
+    if (poolable(c)) members[c->db.type ? 1 : 0].push_back(c);
+  }
+  for (int t = 0; t < 2; t++)
+    if (!members[t].empty()) {
+      int rc = ngia::pool::group_open(members[t], &b->pool[t]);
+      if (rc) {
+        destroy_pool_graph(b);
+        return rc;
+      }
+    }
+  if (!b->pstream) CKB_(cudaStreamCreateWithFlags(&b->pstream, cudaStreamNonBlocking));
+  CKB_(cudaGraphCreate(&b->pgraph, 0));
+  auto add_while = [&](cudaGraph_t *body, cudaGraphConditionalHandle *cond) -> int {
+    CKB_(cudaGraphConditionalHandleCreate(cond, b->pgraph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = *cond;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    CKB_(cudaGraphAddNode(&node, b->pgraph, nullptr, nullptr, 0, &np));
+    *body = np.conditional.phGraph_out[0];
+    return NGIA_OK;
+  };
+  for (int t = 0; t < 2; t++) {
+    if (!b->pool[t]) continue;
+    cudaGraph_t body;
+    cudaGraphConditionalHandle cond;
+    int rc = add_while(&body, &cond);
+    if (rc) {
+      destroy_pool_graph(b);
+      return rc;
+    }
+    CKB_(cudaStreamBeginCaptureToGraph(b->pstream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    rc = ngia::pool::group_enqueue_round(b->pool[t], b->pstream, cond);
+    cudaGraph_t captured = nullptr;
+    cudaError_t e = cudaStreamEndCapture(b->pstream, &captured);
+    if (rc != NGIA_OK || e != cudaSuccess) {
+      destroy_pool_graph(b);
+      return rc != NGIA_OK ? rc : fail(NGIA_E_CUDA, "pool graph capture: %s", cudaGetErrorString(e));
+    }
+  }
+  for (ngia_ctx *c : b->jobs) {
+    if (poolable(c)) continue;
+    cudaGraph_t body;
+    cudaGraphConditionalHandle cond;
+    int rc = add_while(&body, &cond);
+    if (rc) {
+      destroy_pool_graph(b);
+      return rc;
+    }
+    CKB_(cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    rc = ngia::drv::enqueue_iteration(c, true, cond);
+    cudaGraph_t captured = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &captured);
+    if (rc != NGIA_OK || e != cudaSuccess) {
+      destroy_pool_graph(b);
+      return rc != NGIA_OK ? rc : fail(NGIA_E_CUDA, "pool graph capture: %s", cudaGetErrorString(e));
+    }
+  }
+  cudaError_t e = cudaGraphInstantiate(&b->pexec, b->pgraph, 0);
+  if (e != cudaSuccess) {
+    destroy_pool_graph(b);
+    return fail(NGIA_E_CUDA, "pool graph instantiate: %s", cudaGetErrorString(e));
+  }
+  return NGIA_OK;
+}
+
 }  // namespace
 
 extern "C" int ngia_batch_open(const ngia_db_view *jobs, int32_t n_jobs, ngia_batch **out) {
@@ -122,7 +225,8 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
                               int32_t **cluster_out, int32_t **identity_out, ngia_stats *stats) {
   ngia::clear_error();
   if (!b || !params) return fail(NGIA_E_ARG, "ngia_batch_run: bad argument");
-  if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH) return fail(NGIA_E_ARG, "unknown mode %d", mode);
+  if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH && mode != NGIA_MODE_POOL)
+    return fail(NGIA_E_ARG, "unknown mode %d", mode);
   const size_t nj = b->jobs.size();
   if (mode == NGIA_MODE_PLAIN) {
     // one job after the other, host loop per representative
@@ -135,6 +239,35 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
       rc = ngia_cluster_step(c, max_iters, &done);
       if (rc) return rc;
     }
+  } else if (mode == NGIA_MODE_POOL) {
+    // every job is set up on its own stream; the pools' tables are refreshed
+    // with the jobs' run buffers and parameters; one launch runs the batch
+    bool rebuild = !b->pexec || b->pooled.size() != nj;
+    for (size_t j = 0; j < nj; j++) {
+      ngia_ctx *c = b->jobs[j];
+      c->tuned_warp_pairs = 0;
+      int rc = ngia_cluster_begin(c, &params[j], NGIA_MODE_PLAIN);
+      if (rc) return rc;
+      c->mode = NGIA_MODE_GRAPH;
+      c->h_state->iter_limit = max_iters > 0 ? max_iters : INT64_MAX;
+      CKB(cudaMemcpyAsync(&c->rb.st->iter_limit, &c->h_state->iter_limit, sizeof(int64_t),
+                          cudaMemcpyHostToDevice, c->stream));
+      if (!rebuild && (b->pooled[j] != (poolable(c) ? 1 : 0) ||
+                       (!poolable(c) && (!same_prm(b->pprm[j], c->prm) || c->tune_gen != b->ptune[j]))))
+        rebuild = true;
+    }
+    for (size_t j = 0; j < nj; j++) CKB(cudaStreamSynchronize(b->jobs[j]->stream));
+    if (rebuild) {
+      int rc = build_pool_graph(b);
+      if (rc) return rc;
+    }
+    for (auto *g : b->pool)
+      if (g) {
+        int rc = ngia::pool::group_fill(g, b->pstream);
+        if (rc) return rc;
+      }
+    CKB(cudaGraphLaunch(b->pexec, b->pstream));
+    CKB(cudaStreamSynchronize(b->pstream));
   } else {
     // every job is set up (run state reset, iteration limit) on its own
     // stream; then the batch graph runs all of them in one launch
@@ -192,7 +325,9 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
 extern "C" int ngia_batch_close(ngia_batch *b) {
   if (!b) return NGIA_OK;
   destroy_batch_graph(b);
+  destroy_pool_graph(b);
   if (b->stream) cudaStreamDestroy(b->stream);
+  if (b->pstream) cudaStreamDestroy(b->pstream);
   for (ngia_ctx *c : b->jobs) ngia_close(c);
   delete b;
   return NGIA_OK;

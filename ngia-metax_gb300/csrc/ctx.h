@@ -3,6 +3,8 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <vector>
+
 #include "../../include/ngia.h"
 #include "common.cuh"
 
@@ -109,4 +111,13 @@ int align_occupancy(int type, int cls, int max_nb);
 int align_threads();
 cudaError_t align_configure(int type, int max_nb);
 cudaError_t filter_configure();
+// pool.cu: the pooled batch form (NGIA_MODE_POOL), one pool per record type
+namespace pool {
+struct Group;
+int group_open(const std::vector<ngia_ctx *> &jobs, Group **out);  // jobs of one type
+int group_fill(Group *g, cudaStream_t s);  // the jobs' current run buffers and parameters
+int group_enqueue_round(Group *g, cudaStream_t s, cudaGraphConditionalHandle cond);
+int group_size(const Group *g);
+void group_close(Group *g);
+}  // namespace pool
 }  // namespace ngia

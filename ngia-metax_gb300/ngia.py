@@ -18,6 +18,7 @@ LIB_PATH = HERE / "_build" / "libngia.so"
 MODE_PLAIN = 0
 MODE_GRAPH = 1
 MODE_SPEC = 2
+MODE_POOL = 3  # batches only: the jobs of one record type share every launch
 
 
 class NgiaError(RuntimeError):
