@@ -55,6 +55,8 @@ def parse():
                     help="dna_small | dna_1m | protein_200k | batch256 | serve | dna_1m_whole")
     ap.add_argument("--batch-jobs", type=int, default=256)
     ap.add_argument("--batch-max-seqs", type=int, default=200000)
+    ap.add_argument("--batch-iters", type=int, default=-1,
+                    help="batch256: greedy iterations per job and step (-1: --iters-per-step, 0: whole jobs)")
     ap.add_argument("--serve-batches", type=int, default=200)
     ap.add_argument("--serve-rate", type=float, default=200.0, help="Poisson arrivals, batches per second")
     ap.add_argument("--serve-slots", type=int, default=16)
@@ -773,17 +775,20 @@ def batch_jobs(args):
 
 
 def run_batch(args, dist: Dist):
-    """Batch arm: every step runs the first S greedy iterations of all jobs,
-    once as one batch (each job's CUDA graph launched on its own stream, one
-    wait for all) and once one job after the other with the plain host-loop
-    driver.  Both return every job's assignment to the host; timed on the
-    host clock around the call (it synchronises)."""
+    """Batch arm: every step runs the first S greedy iterations of all jobs
+    (--batch-iters; 0 = every job to the end) three ways: the pooled form
+    (one graph launch; the jobs of a record type share every launch of a
+    round, with cross-job work queues per length bucket), the per-job-loop
+    form (one graph launch holding one loop per job) and one job after the
+    other with the plain host-loop driver.  All return every job's assignment
+    to the host; timed on the host clock around the call (it synchronises);
+    the assignments of the three forms are compared."""
     import numpy as np
 
     import ngia
 
     ngia.set_device(dist.local)
-    S = args.iters_per_step
+    S = args.iters_per_step if args.batch_iters < 0 else args.batch_iters
     t0 = time.perf_counter()
     jobs = batch_jobs(args)
     t_gen = time.perf_counter() - t0
@@ -791,7 +796,7 @@ def run_batch(args, dist: Dist):
     n_total = sum(db.n for db in dbs)
     arms = {}
     with ngia.Batch(dbs) as b:
-        for mode, name in ((ngia.MODE_GRAPH, "batch"), (ngia.MODE_PLAIN, "plain")):
+        for mode, name in ((ngia.MODE_POOL, "batch"), (ngia.MODE_GRAPH, "loops"), (ngia.MODE_PLAIN, "plain")):
             for _ in range(args.warmup):
                 b.run(params, mode, max_iters=S)
             dist.barrier()
@@ -806,13 +811,14 @@ def run_batch(args, dist: Dist):
             T = dist.reduce(time.perf_counter() - t, "max")
             arms[name] = dict(T=T, cands=dist.reduce(float(cands), "sum"), cells=dist.reduce(float(cells), "sum"),
                               clk=clocks.stop(), out=(cls, ids))
-    same = all(np.array_equal(a, c) for a, c in zip(arms["batch"]["out"][0], arms["plain"]["out"][0])) and \
-        all(np.array_equal(a, c) for a, c in zip(arms["batch"]["out"][1], arms["plain"]["out"][1]))
+    same = all(np.array_equal(a, c) for o in ("plain", "loops")
+               for a, c in zip(arms["batch"]["out"][0] + arms["batch"]["out"][1],
+                               arms[o]["out"][0] + arms[o]["out"][1]))
     for db in dbs:
         db.close()
     if dist.rank != 0:
         return
-    bat, pln = arms["batch"], arms["plain"]
+    bat, pln, lps = arms["batch"], arms["plain"], arms["loops"]
     n_dna = sum(1 for db in dbs if db.type == 0)
     out = {"metric": METRIC, "value": bat["cands"] / bat["T"], "unit": UNIT, "n_gpus": dist.world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * bat["T"] / args.steps,
@@ -823,14 +829,19 @@ def run_batch(args, dist: Dist):
                                   f"log-uniform 1,000-{args.batch_max_seqs:,} per job, DNA lengths log-uniform "
                                   f"100-10,000, protein log-normal(median 380, sigma 0.7), s in {{0.8,0.9,0.95}}, "
                                   f"w={args.word} (clamped per job)",
-                      "iters_per_step": S, "step": f"first {S} greedy iterations of every job",
+                      "iters_per_step": S, "form": "pooled rounds (NGIA_MODE_POOL)",
+                      "step": f"first {S} greedy iterations of every job" if S else "every job clustered to the end",
                       "timing": "host clock around ngia_batch_run (assignments of all jobs returned to host)",
                       "generation_s": round(t_gen, 1)},
            "gcups": bat["cells"] / bat["T"] / 1e9,
            "plain": {"value": pln["cands"] / pln["T"], "ms_per_step": 1e3 * pln["T"] / args.steps,
                      "gcups": pln["cells"] / pln["T"] / 1e9,
                      "form": "jobs one after the other, host loop per representative"},
-           "speedup_vs_plain": pln["T"] / bat["T"], "bit_exact_vs_plain": bool(same),
+           "loops": {"value": lps["cands"] / lps["T"], "ms_per_step": 1e3 * lps["T"] / args.steps,
+                     "gcups": lps["cells"] / lps["T"] / 1e9,
+                     "form": "one graph launch holding one conditional loop per job (NGIA_MODE_GRAPH)"},
+           "speedup_vs_plain": pln["T"] / bat["T"], "speedup_vs_loops": lps["T"] / bat["T"],
+           "bit_exact_vs_plain": bool(same),
            "clocks": bat["clk"], "plain_clocks": pln["clk"]}
     print(json.dumps(out), flush=True)
 

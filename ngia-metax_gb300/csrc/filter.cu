@@ -364,7 +364,14 @@ __device__ __forceinline__ void flush_stats(const RunBufs &rb, unsigned long lon
 #define NGIA_FILTER_WARP_WORD 1
 #endif
 
-template <int P, int kFilterWordsPerWarp>
+// NGIA_FILTER_SPLIT: launches that cannot run the short-word test in the
+// filter (alignment-first order, the exact short-word path) use an instance
+// compiled without it (kWord = false): each CTA runs its code once, so the
+// kernel's size is paid in instruction fetches.
+#ifndef NGIA_FILTER_SPLIT
+#define NGIA_FILTER_SPLIT 1
+#endif
+template <int P, int kFilterWordsPerWarp, bool kWord = true>
 __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams prm, int exact) {
   constexpr int kFilterTileWords = 8 * kFilterWordsPerWarp;  // 256 threads
   RunState *st = rb.st;
@@ -384,7 +391,7 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
   if (threadIdx.x < A) s_rc[threadIdx.x] = rb.rep_rec[2 + threadIdx.x];
   __syncthreads();
   if (s_hdr[0]) return;
-  const int L1 = s_hdr[1], nb1 = s_hdr[2], word_here = s_hdr[3];
+  const int L1 = s_hdr[1], nb1 = s_hdr[2], word_here = kWord ? s_hdr[3] : 0;
   const int list_words = max(1, (int)((1u << (prm.w * (P == 2 ? 2 : 5))) / 32u));
   // byte table of the k-mer bitset, right after the bitset
   uint8_t *s_tab = reinterpret_cast<uint8_t *>(s_list + list_words);
@@ -733,21 +740,21 @@ cudaError_t launch_filter(ngia_ctx *c) {
       }
     } else if (c->filter_tile == kW) {  // the tuner's choice: one bitmap word per warp and tile
       if (P == 2)
-        k_filter<2, kW><<<grid_w, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
+        k_filter<2, kW, !NGIA_FILTER_SPLIT><<<grid_w, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
       else
-        k_filter<5, kW><<<grid_w, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
+        k_filter<5, kW, !NGIA_FILTER_SPLIT><<<grid_w, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
     } else {
       if (P == 2)
-        k_filter<2, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
+        k_filter<2, kB, !NGIA_FILTER_SPLIT><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
       else
-        k_filter<5, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
+        k_filter<5, kB, !NGIA_FILTER_SPLIT><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 0);
     }
     return cudaGetLastError();
   }
   if (P == 2)
-    k_filter<2, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
+    k_filter<2, kB, !NGIA_FILTER_SPLIT><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
   else
-    k_filter<5, kB><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
+    k_filter<5, kB, !NGIA_FILTER_SPLIT><<<grid_b, 256, smem, c->stream>>>(c->db, c->rb, c->prm, 1);
   k_scan_words<<<1, 1024, 0, c->stream>>>(reinterpret_cast<const uint32_t *>(c->rb.flags), nbw, c->rb.scan_part);
   k_first_short<<<64, 256, 0, c->stream>>>(c->db, c->rb, 1);
   k_first_short<<<c->num_sms * 2, 256, 0, c->stream>>>(c->db, c->rb, 0);

@@ -75,6 +75,7 @@ struct PoolDev {
 
 constexpr int kPoolWarpWordLen = 2048;  // longer candidates are word-counted by a whole warp
 constexpr int kPoolMaxJobs = 8192;       // the filter keeps the word prefix in shared memory
+static_assert(sizeof(PoolJob) % 4 == 0, "job entries are copied as words");
 
 // Copies a job's table entry into shared memory with the whole CTA.
 __device__ __forceinline__ void load_job(const PoolJob *src, PoolJob *dst) {
@@ -89,8 +90,14 @@ __device__ __forceinline__ bool job_running(const RunState *st) {
 }
 
 // ---- prep -------------------------------------------------------------------
+// Shared storage for one job's table entry (raw words: the entry is copied
+// in by load_job, nothing is constructed).
+#define NGIA_POOL_SHARED_JOB(name)                                            \
+  __shared__ __align__(16) uint32_t name##_raw[sizeof(PoolJob) / 4];          \
+  PoolJob &name = *reinterpret_cast<PoolJob *>(name##_raw)
+
 __global__ void __launch_bounds__(512) k_pool_prep(PoolDev pd) {
-  __shared__ __align__(16) PoolJob s_job;
+  NGIA_POOL_SHARED_JOB(s_job);
   const int j = blockIdx.x;
   load_job(pd.jobs + j, &s_job);
   prep_body(s_job.db, s_job.rb, s_job.prm, -1);
@@ -596,7 +603,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P)) k_pool_ali
 
 // ---- next representative, loop condition -----------------------------------------
 __global__ void __launch_bounds__(1024) k_pool_next(PoolDev pd) {
-  __shared__ __align__(16) PoolJob s_job;
+  NGIA_POOL_SHARED_JOB(s_job);
   load_job(pd.jobs + blockIdx.x, &s_job);
   next_body(s_job.db, s_job.rb, 0ull, 0);
 }

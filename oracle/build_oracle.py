@@ -72,9 +72,26 @@ def build_ref() -> Path | None:
     return exe
 
 
+def stage_ref_program() -> None:
+    """Copies the reference's CUDA clustering sources into baseline/_ref
+    (the git-ignored directory that travels to GPU hosts) when the reference
+    tree is present and they are not staged yet; see ref_cluster.py."""
+    if not (REFERENCE / "CUDA" / "signalNode" / "src" / "func.cu").exists():
+        return
+    import sys
+
+    if str(HERE.parent) not in sys.path:
+        sys.path.insert(0, str(HERE.parent))
+    from oracle import ref_cluster
+
+    if not (ref_cluster.STAGE / "src" / "func.cu").exists():
+        ref_cluster.stage()
+
+
 def build() -> None:
     build_oracle()
     build_ref()
+    stage_ref_program()
 
 
 if __name__ == "__main__":
