@@ -86,7 +86,9 @@
 //    small widths), so when every busy lane of the warp fills the warp's
 //    tiles exactly (no padding slot above its window) the block's growth is
 //    the popcount of the last tile's carry-out word; otherwise the window is
-//    recounted from the ring.
+//    recounted from the ring.  Off: on GB300 (1M DNA, s=0.85) it ran at
+//    0.99x (7.11 vs 7.07 ms per launch); the warp vote and the recounts of
+//    windows that do not fill their tiles cost more than the popcounts saved.
 #ifndef NGIA_EQ_ZCARRY
 #define NGIA_EQ_ZCARRY 0
 #endif
