@@ -8,6 +8,8 @@
 #pragma once
 #include <stdint.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "kmer.cuh"
 #include "tile.cuh"
@@ -161,18 +163,36 @@ __global__ void __launch_bounds__(256) k_serve_filter(DevDB qdb, RepStore rs, Ru
   }
 }
 
+// NGIA_SERVE_STAGE (DNA): each warp copies the match table of the
+// representative its pairs use into its own shared-memory region and runs
+// the tiles with the FMA-pipe bookkeeping of the clustering kernel
+// (tile.cuh); the claimed pairs start in groups that share a representative.
+// 0: every lane reads its pair's table from global memory.
+#ifndef NGIA_SERVE_STAGE
+#define NGIA_SERVE_STAGE 1
+#endif
+
 // Banded LCS of the queued (representative, query) pairs of one class: the
 // loop of k_align_tiled (align.cu) with the representative taken per pair.
 // MASK = false: first match (rb.key keeps the smallest accepting rep per
 // query, pairs of larger reps are skipped once a smaller one accepted);
 // MASK = true: every pair runs and an accepted one sets bit r of rb.mask[q]
 // and its score.
+// A warp claims 32 queue entries once none of its lanes holds a pair.  With
+// staging (DNA), the claimed pairs start in groups: each group is the lanes
+// whose pair has the representative of the first waiting lane, that
+// representative's table is copied into the warp's region unless it is
+// there already, and the next group starts when the current one is done.
+// The filters queue the pairs of one representative next to each other (one
+// CTA per representative in serving, per-candidate pushes in the
+// speculative rounds), so a claim holds one or two groups.
 template <int P, int RING, bool MASK>
 __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
     k_serve_align(DevDB qdb, RepStore rs, RunParams prm, RoundBufs rb, int cls, int word_after, uint32_t *scratch,
                   int64_t scratch_words, uint32_t ring_mask) {
   extern __shared__ __align__(16) uint32_t smem[];
   __shared__ uint32_t s_qn;
+  constexpr bool kStage = P == 2 && NGIA_SERVE_EQ && NGIA_SERVE_STAGE;
   if (threadIdx.x == 0) s_qn = (int64_t)rb.ctl[cls] < rb.cap ? rb.ctl[cls] : (uint32_t)rb.cap;
   __syncthreads();
   const uint32_t qn = s_qn;
@@ -187,10 +207,19 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
     ring.mask = ring_mask;
     ring.stride = TL;
   }
+  // this warp's match-table region (after the shared ring)
+  uint32_t *w_eq = smem + (RING > 0 ? RING * kAlignThreads : 0) + (int64_t)(threadIdx.x >> 5) * rs.eq_stride;
+  const uint32_t w_eq_s = smem_u32(w_eq);
+  (void)w_eq_s;
+  // 1 and 4 as values ptxas cannot fold (the FMA-pipe bookkeeping of tile.cuh)
+  const uint32_t one_rt = 1u + (uint32_t)(qn == 0u);
+  const FmaK fk{one_rt, one_rt << 2};
+  (void)fk;
+  int staged = -1;  // representative whose table is in the warp's region (warp-uniform)
   const int lane = threadIdx.x & 31;
   const float s = prm.s;
   const int hw = qdb.hw;
-  int state = -1;
+  int state = -1;  // -1 idle, -2 queue exhausted, >= 0 a claimed entry (waiting or running)
   int r = 0, q = 0, i = 0, nq = 0, B = 0, js = 0, je = -1, net1 = 0, nb1 = 0, net2 = 0, L2 = 0, cutoff = 0;
   int lastcols = 32, frozen = 0, zw = 0;
   uint32_t vlast = 0;
@@ -198,19 +227,20 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
   const uint32_t *qpl = nullptr, *rpl = nullptr;
   uint32_t cur[P], nxt[P];
   unsigned long long n_pairs = 0, n_cells = 0;
-  // every loop pass advances a busy lane by one query block or claims:
-  // bounded by the queued pairs' blocks (each at most kMaxBlocks) per warp
-  const long long guard_max = ((long long)qn + 64) * (kMaxBlocks + 4);
+  // every loop pass advances a running lane by one query block, claims, or
+  // starts a group: bounded by the queued pairs' blocks (each at most
+  // kMaxBlocks) and the groups per claim, per warp
+  const long long guard_max = ((long long)qn + 64) * (kMaxBlocks + 36);
   long long guard = 0;
   for (;;) {
     if (++guard > guard_max) {
       if (lane == 0) atomicExch(&rb.ctl[7], 1u);
       break;
     }
-    {  // refill once every lane is idle (lockstep, as in k_align_tiled); the
+    {  // refill once no lane holds a pair (lockstep, as in k_align_tiled); the
        // warp vote runs on all 32 lanes before it is combined per lane
-      const bool any_busy = __any_sync(kFullMask, state >= 0);
-      const bool need = state == -1 && !any_busy;
+      const bool any_held = __any_sync(kFullMask, state >= 0);
+      const bool need = state == -1 && !any_held;
       const unsigned nm = __ballot_sync(kFullMask, need);
       if (nm) {
         const int leader = __ffs(nm) - 1;
@@ -220,55 +250,74 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
         if (need) {
           const uint32_t idx = base + (uint32_t)__popc(nm & ((1u << lane) - 1u));
           state = idx < qn ? (int)idx : -2;
+          if (state >= 0) {
+            const int2 e = rb.queue[cls][state];
+            r = e.x;
+            q = e.y;
+          }
         }
       }
     }
     if (__all_sync(kFullMask, state == -2)) break;
-    bool busy = state >= 0;
-    if (busy && !active) {
-      const int2 e = rb.queue[cls][state];
-      r = e.x;
-      q = e.y;
-      const uint32_t *rrec = rs.words + rs.off[r];
-      const int L1 = (int)rrec[0];
-      net1 = (int)rrec[1];
-      nb1 = (net1 + 31) >> 5;
-      rpl = rrec + hw;
-      vlast = (net1 & 31) ? ((1u << (net1 & 31)) - 1u) : 0xFFFFFFFFu;
-      L2 = __ldg(qdb.len + q);
-      net2 = __ldg(qdb.net + q);
-      nq = (net2 + 31) >> 5;
-      lastcols = (net2 & 31) ? (net2 & 31) : 32;
-      B = band_blocks(L1, L2, s);
-      cutoff = cutoff_of(L2, s);
-      qpl = qdb.words + __ldg(qdb.off + q) + hw;
-      i = 0;
-      js = 0;
-      je = min(B, nb1 - 1);
-      frozen = 0;
-      zw = 0;
-      if (!MASK && (rb.key[q] >> 32) < (unsigned long long)r) {
-        state = -1;  // a smaller representative already holds q
-        busy = false;
-      } else if (B < 0 || je < 0 || nq == 0) {
-        if (!(0 < cutoff)) {
-          if (MASK) {
-            rb.score[(int64_t)r * rb.score_stride + q] = 0;
-            atomicOr(&rb.mask[q], 1ull << r);
-          } else {
-            atomicMin(&rb.key[q], (unsigned long long)r << 32);
+    // start the next group once no pair runs
+    if (!__any_sync(kFullMask, active)) {
+      const unsigned pm = __ballot_sync(kFullMask, state >= 0);
+      int rg = r;
+      if constexpr (kStage) {
+        if (pm) {
+          rg = __shfl_sync(kFullMask, r, __ffs(pm) - 1);
+          if (rg != staged) {
+            const uint32_t *rrec = rs.words + rs.off[rg];
+            const int words = 4 * (((int)rrec[1] + 31) / 32 + kEqPad);  // table blocks + zero blocks
+            const uint4 *src = reinterpret_cast<const uint4 *>(rs.eq + (int64_t)rg * rs.eq_stride);
+            __syncwarp();
+            for (int t = lane; t < words / 4; t += 32) reinterpret_cast<uint4 *>(w_eq)[t] = __ldg(src + t);
+            __syncwarp();
+            staged = rg;
           }
         }
-        state = -1;
-        busy = false;
-      } else {
-        for (int j = 0; j <= je; j++) ring[j] = 0xFFFFFFFFu;
+      }
+      if (state >= 0 && r == rg) {
+        const uint32_t *rrec = rs.words + rs.off[r];
+        const int L1 = (int)rrec[0];
+        net1 = (int)rrec[1];
+        nb1 = (net1 + 31) >> 5;
+        rpl = rrec + hw;
+        vlast = (net1 & 31) ? ((1u << (net1 & 31)) - 1u) : 0xFFFFFFFFu;
+        L2 = __ldg(qdb.len + q);
+        net2 = __ldg(qdb.net + q);
+        nq = (net2 + 31) >> 5;
+        lastcols = (net2 & 31) ? (net2 & 31) : 32;
+        B = band_blocks(L1, L2, s);
+        cutoff = cutoff_of(L2, s);
+        qpl = qdb.words + __ldg(qdb.off + q) + hw;
+        i = 0;
+        js = 0;
+        je = min(B, nb1 - 1);
+        frozen = 0;
+        zw = 0;
+        if (!MASK && (rb.key[q] >> 32) < (unsigned long long)r) {
+          state = -1;  // a smaller representative already holds q
+        } else if (B < 0 || je < 0 || nq == 0) {
+          if (!(0 < cutoff)) {
+            if (MASK) {
+              rb.score[(int64_t)r * rb.score_stride + q] = 0;
+              atomicOr(&rb.mask[q], 1ull << r);
+            } else {
+              atomicMin(&rb.key[q], (unsigned long long)r << 32);
+            }
+          }
+          state = -1;
+        } else {
+          for (int j = 0; j <= je; j++) ring[j] = 0xFFFFFFFFu;
 #pragma unroll
-        for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
-        active = true;
-        n_pairs++;
+          for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
+          active = true;
+          n_pairs++;
+        }
       }
     }
+    const bool busy = active;
     constexpr int MT = tiled_main(P);
     const int n = busy ? je - js + 1 : 0;
     const int full = (int)__reduce_min_sync(kFullMask, busy ? (unsigned)(n / MT) : 0xFFFFFFFFu);
@@ -280,26 +329,42 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 #pragma unroll
       for (int p = 0; p < P; p++) nxt[p] = __ldg(qpl + (i + 1) * P + p);
     }
-    if constexpr (P == 2 && NGIA_SERVE_EQ) {  // match words from the pair's representative's table
-      using Ring = typename RingOf<RING>::T;
-      const uint32_t *req = rs.eq + (int64_t)r * rs.eq_stride;
-      uint32_t q[4];
-      eq_codes(cur, q);
+    using Ring = typename RingOf<RING>::T;
+    if constexpr (kStage) {  // match words from the warp's staged table (shared memory)
+      uint32_t wc[2];
+      eq_codes_top(cur, wc);
       uint32_t cw = 0, ncw = 0;
       int base = js;
+      if (NGIA_EQ_NOZOLD) zw = 0;  // the tiles return their rows' zero counts
       for (int t = 0; t < full; t++, base += MT) {
-        zw += tiled_tile_eq<MT, NGIA_SERVE_PF, Ring>(ring, req, base, je, nb1, cols, q, cw, ncw);
+        zw += tiled_tile_eqf<MT, NGIA_SERVE_PF, Ring>(ring, w_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
         cw = ncw << (32 - cols);
         ncw = 0;
       }
       for (; rem >= MT; rem -= MT, base += MT) {
-        zw += tiled_tile_eq<MT, NGIA_SERVE_PF, Ring>(ring, req, base, je, nb1, cols, q, cw, ncw);
+        zw += tiled_tile_eqf<MT, NGIA_SERVE_PF, Ring>(ring, w_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
         cw = ncw << (32 - cols);
         ncw = 0;
       }
-      if (rem > 0) zw += tiled_rem_eq<Ring, MT>(rem, ring, req, base, je, nb1, cols, q, cw, ncw);
+      if (rem > 0) zw += tiled_rem_eqf<Ring, MT>(rem, ring, w_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+    } else if constexpr (P == 2 && NGIA_SERVE_EQ) {  // match words from the pair's representative's table
+      const uint32_t *req = rs.eq + (int64_t)r * rs.eq_stride;
+      uint32_t q4[4];
+      eq_codes(cur, q4);
+      uint32_t cw = 0, ncw = 0;
+      int base = js;
+      for (int t = 0; t < full; t++, base += MT) {
+        zw += tiled_tile_eq<MT, NGIA_SERVE_PF, Ring>(ring, req, base, je, nb1, cols, q4, cw, ncw);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      for (; rem >= MT; rem -= MT, base += MT) {
+        zw += tiled_tile_eq<MT, NGIA_SERVE_PF, Ring>(ring, req, base, je, nb1, cols, q4, cw, ncw);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      if (rem > 0) zw += tiled_rem_eq<Ring, MT>(rem, ring, req, base, je, nb1, cols, q4, cw, ncw);
     } else {
-      using Ring = typename RingOf<RING>::T;
       uint32_t cw = 0, ncw = 0;
       int base = js;
       for (int t = 0; t < full; t++, base += MT) {
@@ -374,7 +439,32 @@ AlignServeFn serve_align_fn(int type, int cls) {
   return cls == 0 ? k_serve_align<5, 64, MASK> : cls == 1 ? k_serve_align<5, 128, MASK> : k_serve_align<5, 0, MASK>;
 }
 
-inline size_t serve_align_smem(int cls) { return cls == 2 ? 0 : (size_t)(cls == 0 ? 64 : 128) * kAlignThreads * 4; }
+// Dynamic shared memory of class cls: the row ring (shared classes) and, for
+// DNA with staging, one match-table region of eq_stride words per warp.
+inline size_t serve_align_smem(int type, int cls, int64_t eq_stride) {
+  size_t b = cls == 2 ? 0 : (size_t)(cls == 0 ? 64 : 128) * kAlignThreads * 4;
+  if (type == 0 && NGIA_SERVE_EQ && NGIA_SERVE_STAGE) b += 4 * (size_t)(kAlignThreads / 32) * (size_t)eq_stride;
+  return b;
+}
+
+// Raises the kernel's dynamic shared memory limit to `bytes` (never lowers
+// it: launches of other open servers or contexts may need more).
+template <bool MASK>
+cudaError_t serve_align_configure(int type, int cls, size_t bytes) {
+  static std::mutex mu;
+  static size_t have[64][2][kServeClasses] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t &h = have[dev][type ? 1 : 0][cls];
+  if (bytes <= h) return cudaSuccess;
+  e = cudaFuncSetAttribute((const void *)serve_align_fn<MASK>(type, cls), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)bytes);
+  if (e == cudaSuccess) h = bytes;
+  return e;
+}
 
 }  // namespace
 }  // namespace ngia

@@ -230,7 +230,8 @@ int run_batch(ngia_server *sv, Slot &sl, Request &rq) {
       int64_t sw = sl.scratch_words;
       uint32_t rm = sv->ring_mask;
       void *args[] = {&db, &rs, &prm, &rb, &cls, &wa, &scr, &sw, &rm};
-      CKS(cudaLaunchKernel((const void *)fn, dim3(sl.grid[k]), dim3(kAlignThreads), args, serve_align_smem(k), st));
+      CKS(cudaLaunchKernel((const void *)fn, dim3(sl.grid[k]), dim3(kAlignThreads), args,
+                           serve_align_smem(sv->type, k, sv->store.eq_stride), st));
     }
     if (ev[2]) cudaEventRecord(ev[2], st);
     k_serve_round_end<<<std::max(1, std::min(c->num_sms, (nbw + 255) / 256)), 256, 0, st>>>(n, rb);
@@ -382,7 +383,7 @@ int open_slot(ngia_server *sv, Slot &sl, int index) {
   for (int k = 0; k < kServeClasses; k++) {
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void *)serve_align_fn<false>(sv->type, k), kAlignThreads,
-                                                      serve_align_smem(k)) != cudaSuccess ||
+                                                      serve_align_smem(sv->type, k, sv->store.eq_stride)) != cudaSuccess ||
         occ < 1)
       occ = 1;
     sl.grid[k] = sv->num_sms * occ;
@@ -493,9 +494,8 @@ extern "C" int ngia_serve_open(const ngia_db_view *reps, const ngia_params *para
   uint32_t ring = 1;
   while ((int)ring < rc_ctx->db.max_nb) ring <<= 1;
   sv->ring_mask = ring - 1;
-  for (int k = 0; k < 2; k++) {
-    e = cudaFuncSetAttribute((const void *)ngia::serve_align_fn<false>(sv->type, k),
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ngia::serve_align_smem(k));
+  for (int k = 0; k < ngia::kServeClasses; k++) {
+    e = ngia::serve_align_configure<false>(sv->type, k, ngia::serve_align_smem(sv->type, k, sv->store.eq_stride));
     if (e != cudaSuccess) {
       ngia::destroy(sv);
       return fail(NGIA_E_CUDA, "ngia_serve_open: kernel attributes: %s", cudaGetErrorString(e));
@@ -507,7 +507,8 @@ extern "C" int ngia_serve_open(const ngia_db_view *reps, const ngia_params *para
   const int64_t budget = cf.memory_budget > 0 ? cf.memory_budget : (int64_t)(free_b / 2);
   int occ2 = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ2, (const void *)ngia::serve_align_fn<false>(sv->type, 2),
-                                                ngia::kAlignThreads, 0);
+                                                ngia::kAlignThreads,
+                                                ngia::serve_align_smem(sv->type, 2, sv->store.eq_stride));
   const int64_t per = ngia::slot_bytes(sv, sv->num_sms * std::max(1, occ2));
   const int n_slots = (int)std::min<int64_t>(cf.slots, budget / per);
   if (n_slots < 1) {

@@ -378,9 +378,10 @@ int spec_alloc(ngia_ctx *c) {
     std::lock_guard<std::mutex> lock(mu);
     for (int k = 0; k < kServeClasses; k++) {
       const void *fn = (const void *)serve_align_fn<true>(sp->type, k);
-      CKP(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)serve_align_smem(k)));
+      const size_t smem = serve_align_smem(sp->type, k, sp->eq_stride);
+      CKP(serve_align_configure<true>(sp->type, k, smem));
       int occ = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kAlignThreads, serve_align_smem(k)) != cudaSuccess ||
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kAlignThreads, smem) != cudaSuccess ||
           occ < 1)
         occ = 1;
       sp->grid[k] = c->num_sms * occ;
@@ -430,7 +431,7 @@ int spec_launch_round(ngia_ctx *c, bool lists) {
     uint32_t rm = sp->ring_mask;
     void *args[] = {&db, &rs, &prm, &rb, &cls, &wa, &scr, &sw, &rm};
     CKP(cudaLaunchKernel((const void *)serve_align_fn<true>(c->db.type, k), dim3(sp->grid[k]), dim3(kAlignThreads),
-                         args, serve_align_smem(k), st));
+                         args, serve_align_smem(c->db.type, k, sp->eq_stride), st));
   }
   k_spec_resolve<<<1, 32, 0, st>>>(sp->d, sp->rb);
   CKP(cudaGetLastError());
