@@ -163,13 +163,19 @@ __global__ void __launch_bounds__(256) k_serve_filter(DevDB qdb, RepStore rs, Ru
   }
 }
 
-// NGIA_SERVE_STAGE (DNA): each warp copies the match table of the
+// NGIA_SERVE_STAGE 1 (DNA): each warp copies the match table of the
 // representative its pairs use into its own shared-memory region and runs
 // the tiles with the FMA-pipe bookkeeping of the clustering kernel
 // (tile.cuh); the claimed pairs start in groups that share a representative.
-// 0: every lane reads its pair's table from global memory.
+// 0 (default): every lane reads its pair's table from global memory (L1).
+// Measured on GB300: serving 56.5k vs 59.2k queries/s (configuration 5,
+// 16 slots), speculative rounds of the 20,000-sequence job 0.685 vs 0.507 s.
+// The kernel is bound by the ALU pipe (80% busy, loads 50%), so the shared
+// tables save little, while groups leave lanes idle (27.7 of 32 active): a
+// claim holds pairs of several representatives, above all in the
+// speculative rounds, whose queue interleaves the candidates.
 #ifndef NGIA_SERVE_STAGE
-#define NGIA_SERVE_STAGE 1
+#define NGIA_SERVE_STAGE 0
 #endif
 
 // Banded LCS of the queued (representative, query) pairs of one class: the
