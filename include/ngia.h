@@ -139,18 +139,20 @@ typedef struct ngia_ctx ngia_ctx;
 #define NGIA_MODE_GRAPH  1  /* device-side driver in a captured CUDA graph
                                (conditional while node), no host round trip  */
 #define NGIA_MODE_SPEC   2  /* speculative rounds once the unclustered set is
-                               small (<= 524,288 sequences: K >= 2 candidates
-                               with K x unclustered <= 2^20 pairs): the next K
-                               are candidate representatives of one round,
-                               every pair against them runs at once and the
-                               greedy order is replayed on the device (same
-                               result as the one-representative loop); host
-                               loop per round.  Plain iterations while the
-                               set is larger, and throughout when the database
-                               has records of net length < 16, precise is 0
-                               and more than 16,384 sequences (the reference's
-                               short-word kernel then makes a pair's test
-                               depend on its iteration's job list).          */
+                               small (<= 32,768 sequences, K x unclustered <=
+                               2^20 pairs, 2 <= K <= 64): the next K are
+                               candidate representatives of one round, every
+                               pair against them runs at once and the greedy
+                               order is replayed on the device (same result as
+                               the one-representative loop); host loop per
+                               round.  While the set is larger, iterations of
+                               the captured loop (as NGIA_MODE_GRAPH, 8 between
+                               looks at the set), and only those when the
+                               database has records of net length < 16,
+                               precise is 0 and more than 16,384 sequences
+                               (the reference's short-word kernel then makes a
+                               pair's test depend on its iteration's job
+                               list).                                         */
 
 typedef struct ngia_stats {
     int64_t iterations;    /* representatives taken (= clusters)             */

@@ -165,6 +165,15 @@ bool same_params(const ngia::RunParams &a, const ngia::RunParams &b) {
          a.wait_polls == b.wait_polls;
 }
 
+// The captured loop for the context's current parameters and tuning,
+// captured again only when they changed.
+int ensure_graph(ngia_ctx *c) {
+  if (c->graph_ready && same_params(c->graph_prm, c->prm) && c->graph_warp_pairs == c->warp_pairs &&
+      c->graph_tune_gen == c->tune_gen)
+    return NGIA_OK;
+  return build_graph(c);
+}
+
 int validate_params(int type, const ngia_params *p) {
   if (!p) return fail(NGIA_E_ARG, "null params");
   if (!(p->similarity >= 0.1f && p->similarity <= 1.0f))
@@ -504,10 +513,8 @@ int ngia::drv::begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, con
   if (d_alive) CK(ngia::launch_subset_start(c, d_alive));
   rc = pull_state(c);
   if (rc) return rc;
-  if (mode == NGIA_MODE_GRAPH &&
-      !(c->graph_ready && same_params(c->graph_prm, c->prm) && c->graph_warp_pairs == c->warp_pairs &&
-        c->graph_tune_gen == c->tune_gen)) {
-    rc = build_graph(c);
+  if (mode == NGIA_MODE_GRAPH) {
+    rc = ensure_graph(c);
     if (rc) return rc;
   }
   if (mode == NGIA_MODE_SPEC) {

@@ -85,6 +85,7 @@ int reload_ctx(ngia_ctx *c, const ngia_db_view *v);
 int begin_subset(ngia_ctx *c, const ngia_params *p, int32_t mode, const uint32_t *d_alive);
 // graph form of the greedy loop (captured once per parameter set)
 int build_graph(ngia_ctx *c);
+int ensure_graph(ngia_ctx *c);  // build_graph unless the captured one is current
 void destroy_graph(ngia_ctx *c);
 int pull_state(ngia_ctx *c);
 int enqueue_iteration(ngia_ctx *c, bool graph, cudaGraphConditionalHandle cond);

@@ -46,6 +46,14 @@ namespace {
 
 constexpr int kSpecMax = 64;              // candidate representatives per round (one mask bit each)
 constexpr int kSpecBudget = 1 << 20;      // pairs per round at most (K x unclustered)
+// Rounds start once the unclustered set is this small: a one-representative
+// iteration over a larger set fills the GPU, and the round kernels (the
+// representative taken per pair) run at about half the clustering kernels'
+// cell rate (GB300, 1M DNA s=0.85: 7.3 ms for 1M pairs in the clustering
+// kernel; a greedy iteration over 32k sequences is bounded by the latency of
+// its slowest pair, 0.2-0.3 ms).
+constexpr int kSpecMaxAlive = 1 << 15;
+constexpr int kSpecRecheck = 8;  // graph iterations between looks at the unclustered set
 constexpr int64_t kSpecScoreWords = 1ll << 26;  // K x n scores at most (256 MB)
 
 struct SpecCtl {
@@ -80,7 +88,7 @@ __device__ __forceinline__ int block_sum_1024(int v, int *s_red) {
 // record offsets; zeroes the round's queue counters.  Marks the run done when
 // nothing is left.
 __global__ void __launch_bounds__(1024) k_spec_pick(DevDB db, RunBufs run, SpecDev sd, RoundBufs rb, int k_max,
-                                                    int budget) {
+                                                    int budget, int max_alive) {
   __shared__ int s_red[32];
   __shared__ int s_k, s_found;
   RunState *st = run.st;
@@ -98,7 +106,7 @@ __global__ void __launch_bounds__(1024) k_spec_pick(DevDB db, RunBufs run, SpecD
     const int64_t rem = st->iter_limit - st->iter;
     // at least two candidates per round (one is a plain iteration, which
     // the clustering kernels run faster)
-    if (total > 0 && (int64_t)total * 2 <= budget && k_max >= 2 && !st->err && rem > 0) {
+    if (total > 0 && total <= max_alive && (int64_t)total * 2 <= budget && k_max >= 2 && !st->err && rem > 0) {
       k = min(k_max, budget / total);
       k = min(k, total);
       if (rem < k) k = (int)rem;
@@ -318,8 +326,8 @@ struct ngia_spec {
   int64_t eq_stride = 0;      // words per candidate match table
   int grid[ngia::kServeClasses] = {0, 0, 0};
   int budget = ngia::kSpecBudget;  // pairs per round (NGIA_SPEC_BUDGET lowers it)
+  int max_alive = ngia::kSpecMaxAlive;  // rounds once this few are unclustered (NGIA_SPEC_MAX_ALIVE)
   bool big = false;           // the unclustered set was above the round budget at the last check
-  int64_t plain_since_check = 0;
 };
 
 namespace ngia {
@@ -437,7 +445,7 @@ int spec_launch_round(ngia_ctx *c, bool lists) {
   CKP(cudaGetLastError());
   k_spec_assign<<<c->num_sms * 4, 256, 0, st>>>(c->db, c->rb, sp->d, sp->rb);
   CKP(cudaGetLastError());
-  k_spec_pick<<<1, 1024, 0, st>>>(c->db, c->rb, sp->d, sp->rb, sp->k_max, sp->budget);
+  k_spec_pick<<<1, 1024, 0, st>>>(c->db, c->rb, sp->d, sp->rb, sp->k_max, sp->budget, sp->max_alive);
   CKP(cudaGetLastError());
   return NGIA_OK;
 }
@@ -465,10 +473,12 @@ int spec_prepare(ngia_ctx *c) {
   CKP(cudaMemsetAsync(sp->rb.stats, 0, 2 * sizeof(unsigned long long), c->stream));
   CKP(cudaMemsetAsync(sp->d_ctl, 0, kCtlBytes, c->stream));
   sp->big = false;
-  sp->plain_since_check = 0;
   sp->budget = kSpecBudget;
   if (const char *b = getenv("NGIA_SPEC_BUDGET")) sp->budget = std::max(1, std::min(kSpecBudget, atoi(b)));
-  return NGIA_OK;
+  sp->max_alive = kSpecMaxAlive;
+  if (const char *m = getenv("NGIA_SPEC_MAX_ALIVE")) sp->max_alive = std::max(2, atoi(m));
+  // iterations over larger sets run in the captured loop
+  return ensure_graph(c);
 }
 
 void spec_free(ngia_ctx *c) {
@@ -506,20 +516,27 @@ int spec_step(ngia_ctx *c, int64_t max_iters) {
   for (int64_t guard = 0; !c->h_state->done && c->h_state->iter < limit; guard++) {
     if (guard > 2 * (int64_t)c->db.n + 8)
       return fail(NGIA_E_STATE, "spec: more steps than sequences");
-    if (!exact || sp->big) {  // one plain iteration
-      int rc = enqueue_iteration(c, false, 0);
+    if (!exact || sp->big) {
+      // one-representative iterations in the captured loop: the rest of the
+      // step when rounds would not be exact, else a few before the next look
+      // at the unclustered set
+      const int64_t room = limit - c->h_state->iter;
+      const int64_t n_it = exact ? std::min<int64_t>(room, kSpecRecheck) : room;
+      c->h_state->iter_limit = c->h_state->iter + n_it;
+      CKP(cudaMemcpyAsync(&c->rb.st->iter_limit, &c->h_state->iter_limit, sizeof(int64_t), cudaMemcpyHostToDevice,
+                          c->stream));
+      CKP(cudaGraphLaunch(c->graph_exec, c->stream));
+      int rc = pull_state(c);
       if (rc) return rc;
-      rc = pull_state(c);
-      if (rc) return rc;
+      c->h_state->iter_limit = limit;  // the rounds' own limit again
+      CKP(cudaMemcpyAsync(&c->rb.st->iter_limit, &c->h_state->iter_limit, sizeof(int64_t), cudaMemcpyHostToDevice,
+                          c->stream));
       picked = false;
-      if (exact && ++sp->plain_since_check >= 8) {
-        sp->big = false;  // look at the unclustered set again
-        sp->plain_since_check = 0;
-      }
+      if (exact) sp->big = false;  // look at the unclustered set again
       continue;
     }
     if (!picked) {
-      k_spec_pick<<<1, 1024, 0, c->stream>>>(c->db, c->rb, sp->d, sp->rb, sp->k_max, sp->budget);
+      k_spec_pick<<<1, 1024, 0, c->stream>>>(c->db, c->rb, sp->d, sp->rb, sp->k_max, sp->budget, sp->max_alive);
       CKP(cudaGetLastError());
       int rc = spec_read(c);
       if (rc) return rc;
