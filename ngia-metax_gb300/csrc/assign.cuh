@@ -243,10 +243,13 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       if (lane == 0) atomicExch(&rb.ctl[7], 1u);
       break;
     }
-    {  // refill once no lane holds a pair (lockstep, as in k_align_tiled); the
-       // warp vote runs on all 32 lanes before it is combined per lane
+    {  // refill once prm.refill lanes are idle or none holds a pair (as in
+       // k_align_tiled; with staging only when none holds a pair); the warp
+       // votes run on all 32 lanes before they are combined per lane
       const bool any_held = __any_sync(kFullMask, state >= 0);
-      const bool need = state == -1 && !any_held;
+      const unsigned idle = __ballot_sync(kFullMask, state == -1);
+      const bool refill_now = !any_held || (!kStage && __popc(idle) >= prm.refill);
+      const bool need = state == -1 && refill_now;
       const unsigned nm = __ballot_sync(kFullMask, need);
       if (nm) {
         const int leader = __ffs(nm) - 1;
@@ -265,13 +268,15 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       }
     }
     if (__all_sync(kFullMask, state == -2)) break;
-    // start the next group once no pair runs
-    if (!__any_sync(kFullMask, active)) {
-      const unsigned pm = __ballot_sync(kFullMask, state >= 0);
-      int rg = r;
-      if constexpr (kStage) {
+    // start claimed pairs: without staging at once; with staging in groups
+    // sharing a representative, the next group once no pair runs
+    bool start = state >= 0 && !active;
+    if constexpr (kStage) {
+      start = false;
+      if (!__any_sync(kFullMask, active)) {
+        const unsigned pm = __ballot_sync(kFullMask, state >= 0);
         if (pm) {
-          rg = __shfl_sync(kFullMask, r, __ffs(pm) - 1);
+          const int rg = __shfl_sync(kFullMask, r, __ffs(pm) - 1);
           if (rg != staged) {
             const uint32_t *rrec = rs.words + rs.off[rg];
             const int words = 4 * (((int)rrec[1] + 31) / 32 + kEqPad);  // table blocks + zero blocks
@@ -281,46 +286,47 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
             __syncwarp();
             staged = rg;
           }
+          start = state >= 0 && r == rg;
         }
       }
-      if (state >= 0 && r == rg) {
-        const uint32_t *rrec = rs.words + rs.off[r];
-        const int L1 = (int)rrec[0];
-        net1 = (int)rrec[1];
-        nb1 = (net1 + 31) >> 5;
-        rpl = rrec + hw;
-        vlast = (net1 & 31) ? ((1u << (net1 & 31)) - 1u) : 0xFFFFFFFFu;
-        L2 = __ldg(qdb.len + q);
-        net2 = __ldg(qdb.net + q);
-        nq = (net2 + 31) >> 5;
-        lastcols = (net2 & 31) ? (net2 & 31) : 32;
-        B = band_blocks(L1, L2, s);
-        cutoff = cutoff_of(L2, s);
-        qpl = qdb.words + __ldg(qdb.off + q) + hw;
-        i = 0;
-        js = 0;
-        je = min(B, nb1 - 1);
-        frozen = 0;
-        zw = 0;
-        if (!MASK && (rb.key[q] >> 32) < (unsigned long long)r) {
-          state = -1;  // a smaller representative already holds q
-        } else if (B < 0 || je < 0 || nq == 0) {
-          if (!(0 < cutoff)) {
-            if (MASK) {
-              rb.score[(int64_t)r * rb.score_stride + q] = 0;
-              atomicOr(&rb.mask[q], 1ull << r);
-            } else {
-              atomicMin(&rb.key[q], (unsigned long long)r << 32);
-            }
+    }
+    if (start) {
+      const uint32_t *rrec = rs.words + rs.off[r];
+      const int L1 = (int)rrec[0];
+      net1 = (int)rrec[1];
+      nb1 = (net1 + 31) >> 5;
+      rpl = rrec + hw;
+      vlast = (net1 & 31) ? ((1u << (net1 & 31)) - 1u) : 0xFFFFFFFFu;
+      L2 = __ldg(qdb.len + q);
+      net2 = __ldg(qdb.net + q);
+      nq = (net2 + 31) >> 5;
+      lastcols = (net2 & 31) ? (net2 & 31) : 32;
+      B = band_blocks(L1, L2, s);
+      cutoff = cutoff_of(L2, s);
+      qpl = qdb.words + __ldg(qdb.off + q) + hw;
+      i = 0;
+      js = 0;
+      je = min(B, nb1 - 1);
+      frozen = 0;
+      zw = 0;
+      if (!MASK && (rb.key[q] >> 32) < (unsigned long long)r) {
+        state = -1;  // a smaller representative already holds q
+      } else if (B < 0 || je < 0 || nq == 0) {
+        if (!(0 < cutoff)) {
+          if (MASK) {
+            rb.score[(int64_t)r * rb.score_stride + q] = 0;
+            atomicOr(&rb.mask[q], 1ull << r);
+          } else {
+            atomicMin(&rb.key[q], (unsigned long long)r << 32);
           }
-          state = -1;
-        } else {
-          for (int j = 0; j <= je; j++) ring[j] = 0xFFFFFFFFu;
-#pragma unroll
-          for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
-          active = true;
-          n_pairs++;
         }
+        state = -1;
+      } else {
+        for (int j = 0; j <= je; j++) ring[j] = 0xFFFFFFFFu;
+#pragma unroll
+        for (int p = 0; p < P; p++) cur[p] = __ldg(qpl + p);
+        active = true;
+        n_pairs++;
       }
     }
     const bool busy = active;
