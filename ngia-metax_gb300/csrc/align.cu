@@ -505,11 +505,18 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       uint32_t cw = 0, ncw = 0, last = 0;
       int base = js;
       if (kZC && NGIA_EQ_NOZOLD) zw = 0;  // the tiles return their rows' zero counts
-      for (int t = 0; t < full; t++, base += MT) {
+      // a one-slot remainder joins the last main tile (warp-uniform)
+      const bool merge1 = NGIA_TILED_MERGE1 && rem == 1 && full > 0;
+      for (int t = merge1 ? 1 : 0; t < full; t++, base += MT) {
         zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
         last = ncw;
         cw = ncw << (32 - cols);  // column 0's carry at bit 31
         ncw = 0;
+      }
+      if (merge1) {
+        zw += tiled_tile_eqf<MT + 1, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+        last = ncw;
+        rem = 0;
       }
       for (; rem >= MT; rem -= MT, base += MT) {
         zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);

@@ -89,6 +89,13 @@
 //    recounted from the ring.  Off: on GB300 (1M DNA, s=0.85) it ran at
 //    0.99x (7.11 vs 7.07 ms per launch); the warp vote and the recounts of
 //    windows that do not fill their tiles cost more than the popcounts saved.
+//  NGIA_TILED_MERGE1  1 (with NGIA_EQ_FMA): when a warp's windows leave a
+//    one-slot remainder (the dominant 49-block window of 1M DNA s=0.85 is
+//    16+16+16+1), the last main tile and that slot run as one tile of MT+1
+//    slots, saving a tile's per-column overhead.
+#ifndef NGIA_TILED_MERGE1
+#define NGIA_TILED_MERGE1 0
+#endif
 #ifndef NGIA_EQ_ZCARRY
 #define NGIA_EQ_ZCARRY 0
 #endif
