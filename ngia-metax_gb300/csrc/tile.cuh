@@ -92,7 +92,8 @@
 //  NGIA_TILED_MERGE1  1 (with NGIA_EQ_FMA): when a warp's windows leave a
 //    one-slot remainder (the dominant 49-block window of 1M DNA s=0.85 is
 //    16+16+16+1), the last main tile and that slot run as one tile of MT+1
-//    slots, saving a tile's per-column overhead.
+//    slots, saving a tile's per-column overhead.  Off: 0.99x on GB300
+//    (7.15 vs 7.07 ms per launch, 1M DNA s=0.85).
 #ifndef NGIA_TILED_MERGE1
 #define NGIA_TILED_MERGE1 0
 #endif
