@@ -371,6 +371,11 @@ __device__ __forceinline__ void flush_stats(const RunBufs &rb, unsigned long lon
 #ifndef NGIA_FILTER_SPLIT
 #define NGIA_FILTER_SPLIT 1
 #endif
+// NGIA_FILTER_HOIST: in the composition-only DNA instance, load every header
+// of the warp's words before the first test.
+#ifndef NGIA_FILTER_HOIST
+#define NGIA_FILTER_HOIST 1
+#endif
 template <int P, int kFilterWordsPerWarp, bool kWord = true>
 __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams prm, int exact) {
   constexpr int kFilterTileWords = 8 * kFilterWordsPerWarp;  // 256 threads
@@ -475,6 +480,25 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
       const int wi = word_of(tile, warp * kFilterWordsPerWarp + k);
       bits_of[k] = wi < nbw ? rb.alive[wi] : 0u;
     }
+    // Composition-only DNA instance: the headers of all the warp's words are
+    // loaded before any test (predicated on the unclustered bit), so a warp
+    // waits for one round of loads rather than one per word.
+    constexpr bool kHoist = NGIA_FILTER_HOIST && !kWord && P == 2;
+    constexpr int kH = kHoist ? kFilterWordsPerWarp : 1;
+    int len_h[kH];
+    uint4 cnt_h[kH];
+    if constexpr (kHoist) {
+#pragma unroll
+      for (int k = 0; k < kFilterWordsPerWarp; k++) {
+        const int c = word_of(tile, warp * kFilterWordsPerWarp + k) * 32 + lane;
+        len_h[k] = 0;
+        cnt_h[k] = make_uint4(0u, 0u, 0u, 0u);
+        if ((bits_of[k] >> lane) & 1u) {
+          len_h[k] = __ldg(db.len + c);
+          cnt_h[k] = __ldg(reinterpret_cast<const uint4 *>(db.cnt) + c);
+        }
+      }
+    }
     unsigned pass_of = 0;  // bit k: this lane's candidate of word k survives
 #pragma unroll
     for (int k = 0; k < kFilterWordsPerWarp; k++) {
@@ -488,8 +512,16 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
       if (alive) {
         cand++;
         bytes += 4 * (2 + A);
-        const int L2 = __ldg(db.len + c);
-        pass = !(base_sum<A>(db.cnt, c, s_rc) < cutoff_of(L2, s));
+        int L2, sum;
+        if constexpr (kHoist) {
+          L2 = len_h[k];
+          const uint4 q = cnt_h[k];
+          sum = (int)(min(q.x, s_rc[0]) + min(q.y, s_rc[1]) + min(q.z, s_rc[2]) + min(q.w, s_rc[3]));
+        } else {
+          L2 = __ldg(db.len + c);
+          sum = base_sum<A>(db.cnt, c, s_rc);
+        }
+        pass = !(sum < cutoff_of(L2, s));
         if (pass) base++;
         if (pass && word_here) {
           const int net2 = __ldg(db.net + c);
