@@ -496,7 +496,7 @@ def run_secondary(args, dist, int_gops: float, peaks: dict) -> dict:
     the 200k-protein workload at s=0.9 (value and alignment roofline), the
     serving loop (latency, capacity, oracle replay), the reference's own
     CUDA program beside the drop-in tool on the 20,000-sequence DNA
-    configuration (whole program, outputs byte-compared) and a batch of 64
+    configuration (whole program, outputs byte-compared) and a batch of 32
     independent jobs clustered to the end in the pooled, per-job-loop and
     plain forms (assignments compared)."""
     import ngia
@@ -534,8 +534,8 @@ def run_secondary(args, dist, int_gops: float, peaks: dict) -> dict:
     out["reference_gpu"] = reference_gpu_compare(args)
     out["reference_gpu_s"] = round(time.perf_counter() - t0, 1)
     t0 = time.perf_counter()
-    try:  # a bounded batch: 64 jobs of at most 4,000 sequences, clustered to the end
-        ba = argparse.Namespace(**{**vars(args), "workload": "batch64", "batch_jobs": 64, "batch_max_seqs": 4000,
+    try:  # a bounded batch: 32 jobs of at most 4,000 sequences, clustered to the end
+        ba = argparse.Namespace(**{**vars(args), "workload": "batch32", "batch_jobs": 32, "batch_max_seqs": 4000,
                                    "batch_iters": 0, "steps": 1, "warmup": 1})
         r = run_batch(ba, dist, emit=False)
         out["batch"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "gcups", "plain", "loops", "speedup_vs_plain",
@@ -1011,9 +1011,11 @@ def run_serve(args, dist: Dist, emit: bool = True):
 
 def main():
     args = parse()
-    # hardware queues for the job / slot / class streams (the default is 8);
-    # set before the first CUDA call of the process
-    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+    if args.workload.startswith("batch") or args.workload == "serve":
+        # one hardware queue per job / slot stream (the default is 8); set
+        # before the first CUDA call.  The default run keeps the default, and
+        # so do the programs it starts (the reference comparison).
+        os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     dist = Dist()
     try:
         if args.cpu_only:

@@ -225,8 +225,7 @@ int ngia_batch_open(const ngia_db_view *jobs, int32_t n_jobs, ngia_batch **out);
  * one conditional while node per job, side by side, so jobs run
  * concurrently with no host round trip per representative;
  * NGIA_MODE_POOL: one launch of one CUDA graph holding one while node per
- * record type and length class (longest record up to 2,048 residues, or
- * longer): each round prepares every job's representative, filters the
+ * record type: each round prepares every job's representative, filters the
  * unclustered sequences of all jobs in one launch into each job's length
  * buckets (alignment classes), and aligns each bucket across all jobs in one
  * persistent launch whose CTAs claim chunks of pairs from any job and stage

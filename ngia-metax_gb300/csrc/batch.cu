@@ -40,10 +40,9 @@ struct ngia_batch {
   std::vector<ngia::RunParams> prm;  // each job's parameters the graph was captured with
   std::vector<int> warp_pairs, tune_gen;
   cudaStream_t stream = nullptr;  // the batch graph's launch stream
-  // the pooled form: per record type one pool of the jobs whose records are
-  // at most kPoolShortBlocks blocks long and one of the others, and its graph
-  // (one WHILE node per pool plus one per job the pools do not take)
-  ngia::pool::Group *pool[4] = {nullptr, nullptr, nullptr, nullptr};
+  // the pooled form: one pool per record type, and its graph (one WHILE node
+  // per pool plus one per job the pools do not take)
+  ngia::pool::Group *pool[2] = {nullptr, nullptr};
   cudaGraph_t pgraph = nullptr;
   cudaGraphExec_t pexec = nullptr;
   std::vector<int> pooled;                // per job: 1 in its type's pool, 0 own node
@@ -125,25 +124,25 @@ void destroy_pool_graph(ngia_batch *b) {
 // short-word path (no record of net length < 16 while the test is on).
 bool poolable(const ngia_ctx *c) { return !(c->db.has_short && !c->prm.precise); }
 
-// Pools: by record type and by the longest record.  A pooled round ends with
-// its slowest pair, and one pair of two 10,000-residue records takes
-// milliseconds, so jobs of short records get their own pool (its own loop,
-// running beside the other pools).
-constexpr int kPoolShortBlocks = 64;  // 2,048 residues
-int pool_of(const ngia_ctx *c) { return 2 * (c->db.type ? 1 : 0) + (c->db.max_nb > kPoolShortBlocks ? 1 : 0); }
+// Pools: one per record type.  (Splitting each type by its longest record,
+// so that jobs of short records need not wait for the slowest pair of a
+// round, was measured slower on GB300: 15.2M against 16.5M candidate seqs/s
+// on the 256-job batch, 8 iterations per job; the pools' persistent grids
+// then compete for the GPU.)
+int pool_of(const ngia_ctx *c) { return c->db.type ? 1 : 0; }
 
 // The pooled graph: one WHILE node per non-empty pool (its body is one round
 // of the pool) and one per job outside the pools (its own iteration).
 int build_pool_graph(ngia_batch *b) {
   destroy_pool_graph(b);
-  std::vector<ngia_ctx *> members[4];
+  std::vector<ngia_ctx *> members[2];
   for (ngia_ctx *c : b->jobs) {
     b->pooled.push_back(poolable(c) ? 1 : 0);
     b->pprm.push_back(c->prm);
     b->ptune.push_back(c->tune_gen);
     if (poolable(c)) members[pool_of(c)].push_back(c);
   }
-  for (int t = 0; t < 4; t++)
+  for (int t = 0; t < 2; t++)
     if (!members[t].empty()) {
       int rc = ngia::pool::group_open(members[t], &b->pool[t]);
       if (rc) {
@@ -164,7 +163,7 @@ int build_pool_graph(ngia_batch *b) {
     *body = np.conditional.phGraph_out[0];
     return NGIA_OK;
   };
-  for (int t = 0; t < 4; t++) {
+  for (int t = 0; t < 2; t++) {
     if (!b->pool[t]) continue;
     cudaGraph_t body;
     cudaGraphConditionalHandle cond;
