@@ -205,7 +205,14 @@ int run_batch(ngia_server *sv, Slot &sl, Request &rq) {
   k_serve_init<<<std::max(1, std::min(c->num_sms, (n + 255) / 256)), 256, 0, st>>>(n, rb);
   CKS(cudaGetLastError());
   const int word_after = !sv->word_first && !sv->prm.precise;
-  int r0 = 0, chunk = kFirstChunk;
+  // largest round (NGIA_SERVE_MAX_CHUNK, at most kMaxChunk, which sizes the
+  // slot's pair queues): a query accepted by a representative of a round can
+  // still have its pairs with the round's later representatives aligned
+  static const int max_chunk = [] {
+    const char *m = getenv("NGIA_SERVE_MAX_CHUNK");
+    return m ? std::max(kFirstChunk, std::min(kMaxChunk, atoi(m))) : kMaxChunk;
+  }();
+  int r0 = 0, chunk = std::min(kFirstChunk, max_chunk);
   uint32_t left = (uint32_t)n;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   if (trace())
@@ -255,7 +262,7 @@ int run_batch(ngia_server *sv, Slot &sl, Request &rq) {
               f, a, e);
     }
     r0 += nr;
-    chunk = std::min(chunk * 2, kMaxChunk);
+    chunk = std::min(chunk * 2, max_chunk);
     rq.rounds++;
   }
   for (auto &e : ev)
