@@ -12,16 +12,18 @@
 //                   job: warps take bitmap words of the pool's word space (the
 //                   jobs' bitmaps end to end) and queue survivors into their
 //                   job's length buckets (alignment classes, by band window)
-//   k_pool_chunks   per bucket: the pairs of all jobs cut into chunks, and a
-//                   prefix of chunks over the jobs (the cross-job work queue)
+//                   and, in its last CTA, per bucket: the pairs of all jobs
+//                   cut into chunks and a prefix of chunks over the jobs (the
+//                   cross-job work queue)
 //   k_pool_align    per bucket, one persistent launch: a CTA claims the next
 //                   chunk of the bucket, whichever job it belongs to, stages
 //                   that job's representative (planes, k-mer bitset, DNA
 //                   match table) in shared memory when it differs from the one
 //                   staged, and its lanes run the chunk's pairs through the
 //                   tiled banded LCS (tile.cuh), thread per pair
-//   k_pool_next     one CTA per job: retire the representative, next one
-//   k_pool_cond     any job left: the graph's WHILE condition
+//   k_pool_next     one CTA per job: retire the representative, next one;
+//                   the last CTA sets the graph's WHILE condition (any job
+//                   left)
 //
 // The batch graph (batch.cu) holds one WHILE node per pool (DNA, protein)
 // beside the per-job nodes of jobs the pool does not take: a job whose
@@ -66,6 +68,7 @@ struct PoolDev {
   int32_t *chunk_base;   // kNumClasses x (n_jobs + 1): first chunk of every job, per bucket
   int32_t *chunk_size;   // kNumClasses: pairs per chunk this round
   uint32_t *ctr;         // kNumClasses: chunks claimed this round
+  uint32_t *done;        // [0] filter CTAs finished, [1] next CTAs finished (last one resets)
   uint32_t *scratch;     // global ring of the widest bucket
   int64_t scratch_words;
   uint32_t ring_mask;
@@ -115,6 +118,73 @@ __global__ void __launch_bounds__(512) k_pool_prep(PoolDev pd) {
     H->word_after = act && !st->word_first && st->word_active;
   }
   if (threadIdx.x < s_job.db.A) H->rc[threadIdx.x] = s_job.rb.rep_rec[2 + threadIdx.x];
+}
+
+// ---- chunks -------------------------------------------------------------------
+// Per bucket: the chunk size of this round (about eight chunks per CTA of the
+// bucket's launch, 128 to 4,096 pairs) and the exclusive prefix of every
+// job's chunk count.  Run by the last CTA of the filter (NT threads).
+template <int NT>
+__device__ void chunks_body(const PoolDev &pd, int ncls) {
+  __shared__ long long s_red[NT / 32];
+  __shared__ int32_t s_part[NT];
+  __shared__ int32_t s_C;
+  const int nj = pd.n_jobs, t = threadIdx.x;
+  const int per = (nj + NT - 1) / NT;
+  const int j0 = min(nj, t * per), j1 = min(nj, j0 + per);
+  for (int k = 0; k < ncls; k++) {
+    long long tot = 0;
+    for (int j = j0; j < j1; j++) tot += pd.jobs[j].rb.st->qcount[k];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(kFullMask, tot, o);
+    if ((t & 31) == 0) s_red[t >> 5] = tot;
+    __syncthreads();
+    if (t == 0) {
+      long long T = 0;
+      for (int i = 0; i < NT / 32; i++) T += s_red[i];
+      const long long want = (T + 8ll * pd.grid_align[k] - 1) / (8ll * pd.grid_align[k]);
+      s_C = (int)max(128ll, min(4096ll, want));
+    }
+    __syncthreads();
+    const int C = s_C;
+    int mine = 0;
+    for (int j = j0; j < j1; j++) mine += (int)((pd.jobs[j].rb.st->qcount[k] + C - 1) / C);
+    s_part[t] = mine;
+    __syncthreads();
+    for (int o = 1; o < NT; o <<= 1) {  // inclusive scan of the partials
+      const int v = t >= o ? s_part[t - o] : 0;
+      __syncthreads();
+      s_part[t] += v;
+      __syncthreads();
+    }
+    int32_t *cb = pd.chunk_base + k * (nj + 1);
+    int run = s_part[t] - mine;
+    for (int j = j0; j < j1; j++) {
+      cb[j] = run;
+      run += (int)((pd.jobs[j].rb.st->qcount[k] + C - 1) / C);
+    }
+    if (t == NT - 1) {
+      cb[nj] = s_part[NT - 1];
+      pd.chunk_size[k] = C;
+      pd.ctr[k] = 0;
+    }
+    __syncthreads();
+  }
+}
+
+// True in exactly one CTA of the grid: the last to finish (its view of the
+// other CTAs' global writes is complete after the fence).  Resets *done.
+__device__ __forceinline__ bool last_cta(uint32_t *done) {
+  __shared__ int s_last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(done, 1u) == gridDim.x - 1;
+    if (s_last) *done = 0;  // every other CTA has counted: ready for the next round
+  }
+  __syncthreads();
+  if (s_last) __threadfence();
+  return s_last;
 }
 
 // ---- filter -------------------------------------------------------------------
@@ -167,7 +237,7 @@ __device__ int word_count_warp_bits(const uint32_t *__restrict__ planes, int net
 }
 
 template <int P>
-__global__ void __launch_bounds__(256) k_pool_filter(PoolDev pd) {
+__global__ void __launch_bounds__(256) k_pool_filter(PoolDev pd, int ncls) {
   constexpr int A = P == 2 ? 4 : 28;
   constexpr int type = P == 2 ? 0 : 1;
   extern __shared__ int32_t s_wbase[];  // n_jobs + 1
@@ -248,57 +318,9 @@ __global__ void __launch_bounds__(256) k_pool_filter(PoolDev pd) {
       if (wpass) atomicAdd(f + 4, wpass);
     }
   }
-}
-
-// ---- chunks -------------------------------------------------------------------
-// Per bucket: the chunk size of this round (about eight chunks per CTA of the
-// bucket's launch, 128 to 4,096 pairs) and the exclusive prefix of every
-// job's chunk count.  One CTA of 1,024 threads.
-__global__ void __launch_bounds__(1024) k_pool_chunks(PoolDev pd, int ncls) {
-  __shared__ long long s_red[32];
-  __shared__ int32_t s_part[1024];
-  __shared__ int32_t s_C;
-  const int nj = pd.n_jobs, t = threadIdx.x;
-  const int per = (nj + 1023) / 1024;
-  const int j0 = min(nj, t * per), j1 = min(nj, j0 + per);
-  for (int k = 0; k < ncls; k++) {
-    long long tot = 0;
-    for (int j = j0; j < j1; j++) tot += pd.jobs[j].rb.st->qcount[k];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) tot += __shfl_xor_sync(kFullMask, tot, o);
-    if ((t & 31) == 0) s_red[t >> 5] = tot;
-    __syncthreads();
-    if (t == 0) {
-      long long T = 0;
-      for (int i = 0; i < 32; i++) T += s_red[i];
-      const long long want = (T + 8ll * pd.grid_align[k] - 1) / (8ll * pd.grid_align[k]);
-      s_C = (int)max(128ll, min(4096ll, want));
-    }
-    __syncthreads();
-    const int C = s_C;
-    int mine = 0;
-    for (int j = j0; j < j1; j++) mine += (int)((pd.jobs[j].rb.st->qcount[k] + C - 1) / C);
-    s_part[t] = mine;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {  // inclusive scan of the partials
-      const int v = t >= o ? s_part[t - o] : 0;
-      __syncthreads();
-      s_part[t] += v;
-      __syncthreads();
-    }
-    int32_t *cb = pd.chunk_base + k * (nj + 1);
-    int run = s_part[t] - mine;
-    for (int j = j0; j < j1; j++) {
-      cb[j] = run;
-      run += (int)((pd.jobs[j].rb.st->qcount[k] + C - 1) / C);
-    }
-    if (t == 1023) {
-      cb[nj] = s_part[1023];
-      pd.chunk_size[k] = C;
-      pd.ctr[k] = 0;
-    }
-    __syncthreads();
-  }
+  // the last CTA cuts every bucket's pairs into chunks (the pairs' counts
+  // are final once every CTA has queued its survivors)
+  if (last_cta(pd.done)) chunks_body<256>(pd, ncls);
 }
 
 // ---- alignment -------------------------------------------------------------------
@@ -602,13 +624,13 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P)) k_pool_ali
 }
 
 // ---- next representative, loop condition -----------------------------------------
-__global__ void __launch_bounds__(1024) k_pool_next(PoolDev pd) {
+// One CTA per job; the last CTA to finish sets the loop's condition: any job
+// still running.
+__global__ void __launch_bounds__(1024) k_pool_next(PoolDev pd, cudaGraphConditionalHandle cond) {
   NGIA_POOL_SHARED_JOB(s_job);
   load_job(pd.jobs + blockIdx.x, &s_job);
   next_body(s_job.db, s_job.rb, 0ull, 0);
-}
-
-__global__ void __launch_bounds__(1024) k_pool_cond(PoolDev pd, cudaGraphConditionalHandle cond) {
+  if (!last_cta(pd.done + 1)) return;
   int more = 0;
   for (int j = threadIdx.x; j < pd.n_jobs; j += blockDim.x) more |= job_running(pd.jobs[j].rb.st) ? 1 : 0;
   more = __syncthreads_or(more);
@@ -646,7 +668,7 @@ struct Group {
   PoolJob *d_jobs = nullptr;
   PoolHdr *d_hdr = nullptr;
   int32_t *d_wbase = nullptr, *d_chunk_base = nullptr, *d_chunk_size = nullptr;
-  uint32_t *d_ctr = nullptr, *d_scratch = nullptr;
+  uint32_t *d_ctr = nullptr, *d_scratch = nullptr, *d_done = nullptr;
   cudaStream_t side[kNumClasses] = {nullptr};
   cudaEvent_t fork = nullptr, join[kNumClasses] = {nullptr};
 };
@@ -682,7 +704,7 @@ cudaError_t configure(int type, int max_nb) {
 void group_close(Group *g) {
   if (!g) return;
   for (void *p : {(void *)g->d_jobs, (void *)g->d_hdr, (void *)g->d_wbase, (void *)g->d_chunk_base,
-                  (void *)g->d_chunk_size, (void *)g->d_ctr, (void *)g->d_scratch})
+                  (void *)g->d_chunk_size, (void *)g->d_ctr, (void *)g->d_scratch, (void *)g->d_done})
     if (p) cudaFree(p);
   for (auto &s : g->side)
     if (s) cudaStreamDestroy(s);
@@ -710,7 +732,8 @@ int group_open(const std::vector<ngia_ctx *> &jobs, Group **out) {
   bool ok = dalloc(&g->d_jobs, jobs.size()) == cudaSuccess && dalloc(&g->d_hdr, jobs.size()) == cudaSuccess &&
             dalloc(&g->d_wbase, jobs.size() + 1) == cudaSuccess &&
             dalloc(&g->d_chunk_base, (size_t)kNumClasses * (jobs.size() + 1)) == cudaSuccess &&
-            dalloc(&g->d_chunk_size, kNumClasses) == cudaSuccess && dalloc(&g->d_ctr, kNumClasses) == cudaSuccess;
+            dalloc(&g->d_chunk_size, kNumClasses) == cudaSuccess && dalloc(&g->d_ctr, kNumClasses) == cudaSuccess &&
+            dalloc(&g->d_done, 2) == cudaSuccess && cudaMemset(g->d_done, 0, 2 * sizeof(uint32_t)) == cudaSuccess;
   if (!ok) {
     group_close(g);
     return fail(NGIA_E_NOMEM, "pool: device allocation of the job tables failed");
@@ -762,6 +785,7 @@ int group_open(const std::vector<ngia_ctx *> &jobs, Group **out) {
   pd.chunk_base = g->d_chunk_base;
   pd.chunk_size = g->d_chunk_size;
   pd.ctr = g->d_ctr;
+  pd.done = g->d_done;
   pd.scratch = g->d_scratch;
   pd.n_jobs = nj;
   pd.type = type;
@@ -781,6 +805,7 @@ int group_fill(Group *g, cudaStream_t s) {
     h[j].prm = g->jobs[j]->prm;
   }
   cudaError_t e = cudaMemcpyAsync(g->d_jobs, h.data(), sizeof(PoolJob) * h.size(), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->d_done, 0, 2 * sizeof(uint32_t), s);  // completion counters
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return fail(NGIA_E_CUDA, "pool: table copy: %s", cudaGetErrorString(e));
   return NGIA_OK;
@@ -794,10 +819,9 @@ int group_enqueue_round(Group *g, cudaStream_t s, cudaGraphConditionalHandle con
   k_pool_prep<<<nj, 512, 0, s>>>(pd);
   const size_t fsm = 4 * (size_t)(nj + 1);
   if (type == 0)
-    k_pool_filter<2><<<g->grid_filter, 256, fsm, s>>>(pd);
+    k_pool_filter<2><<<g->grid_filter, 256, fsm, s>>>(pd, nc);
   else
-    k_pool_filter<5><<<g->grid_filter, 256, fsm, s>>>(pd);
-  k_pool_chunks<<<1, 1024, 0, s>>>(pd, nc);
+    k_pool_filter<5><<<g->grid_filter, 256, fsm, s>>>(pd, nc);
   cudaError_t e = cudaEventRecord(g->fork, s);
   for (int k = 0; e == cudaSuccess && k < nc; k++) {
     e = cudaStreamWaitEvent(g->side[k], g->fork, 0);
@@ -811,8 +835,7 @@ int group_enqueue_round(Group *g, cudaStream_t s, cudaGraphConditionalHandle con
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, g->join[k], 0);
   }
   if (e != cudaSuccess) return fail(NGIA_E_CUDA, "pool: alignment launches: %s", cudaGetErrorString(e));
-  k_pool_next<<<nj, 1024, 0, s>>>(pd);
-  k_pool_cond<<<1, 1024, 0, s>>>(pd, cond);
+  k_pool_next<<<nj, 1024, 0, s>>>(pd, cond);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(NGIA_E_CUDA, "pool: launches: %s", cudaGetErrorString(e));
   return NGIA_OK;
