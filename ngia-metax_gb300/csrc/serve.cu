@@ -207,7 +207,10 @@ int run_batch(ngia_server *sv, Slot &sl, Request &rq) {
   const int word_after = !sv->word_first && !sv->prm.precise;
   // largest round (NGIA_SERVE_MAX_CHUNK, at most kMaxChunk, which sizes the
   // slot's pair queues): a query accepted by a representative of a round can
-  // still have its pairs with the round's later representatives aligned
+  // still have its pairs with the round's later representatives aligned.
+  // Swept on GB300 (configuration 5): 1,024, 512, 256 and 128 aligned 300.2M,
+  // 299.3M, 298.5M and 298.0M pairs at 53.1k, 53.0k, 52.3k and 51.3k
+  // queries/s: nearly every pair is one the first-match rule needs.
   static const int max_chunk = [] {
     const char *m = getenv("NGIA_SERVE_MAX_CHUNK");
     return m ? std::max(kFirstChunk, std::min(kMaxChunk, atoi(m))) : kMaxChunk;
