@@ -120,6 +120,14 @@ void destroy_pool_graph(ngia_batch *b) {
   b->ptune.clear();
 }
 
+bool batch_warp() {
+  static const bool on = [] {
+    const char *v = getenv("NGIA_BATCH_WARP");
+    return v && atoi(v) != 0;
+  }();
+  return on;
+}
+
 // A job the pools can take: its greedy loop needs no per-job exact
 // short-word path (no record of net length < 16 while the test is on).
 bool poolable(const ngia_ctx *c) { return !(c->db.has_short && !c->prm.precise); }
@@ -283,8 +291,9 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
       ngia_ctx *c = b->jobs[j];
       // jobs running side by side fill the GPU: one thread per pair, the
       // form with the fewest instructions per cell (256-job batch on GB300:
-      // 15.4M vs 13.0M candidate seqs/s with warp-per-pair classes)
-      c->tuned_warp_pairs = 0;
+      // 15.4M vs 13.0M candidate seqs/s with warp-per-pair classes);
+      // NGIA_BATCH_WARP=1 keeps each job's own warp-per-pair cut-off
+      c->tuned_warp_pairs = batch_warp() ? -1 : 0;
       int rc = ngia_cluster_begin(c, &params[j], NGIA_MODE_PLAIN);  // no per-job graph
       if (rc) return rc;
       c->mode = NGIA_MODE_GRAPH;
