@@ -538,8 +538,8 @@ def run_secondary(args, dist, int_gops: float, peaks: dict) -> dict:
         ba = argparse.Namespace(**{**vars(args), "workload": "batch32", "batch_jobs": 32, "batch_max_seqs": 4000,
                                    "batch_iters": 0, "steps": 1, "warmup": 1})
         r = run_batch(ba, dist, emit=False)
-        out["batch"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "gcups", "plain", "loops", "speedup_vs_plain",
-                                          "speedup_vs_loops", "bit_exact_vs_plain")}
+        out["batch"] = {k: r[k] for k in ("value", "unit", "ms_per_step", "gcups", "plain", "loops", "rounds",
+                                          "speedup_vs_plain", "speedup_vs_loops", "bit_exact_vs_plain")}
         out["batch"]["workload"] = r["config"]["workload"]
         out["batch"]["form"] = r["config"]["form"] + ", every job clustered to the end"
     except Exception as e:
@@ -810,7 +810,8 @@ def run_batch(args, dist: Dist, emit: bool = True):
     n_total = sum(db.n for db in dbs)
     arms = {}
     with ngia.Batch(dbs) as b:
-        for mode, name in ((ngia.MODE_POOL, "batch"), (ngia.MODE_GRAPH, "loops"), (ngia.MODE_PLAIN, "plain")):
+        for mode, name in ((ngia.MODE_POOL, "batch"), (ngia.MODE_GRAPH, "loops"), (ngia.MODE_SPEC, "rounds"),
+                           (ngia.MODE_PLAIN, "plain")):
             for _ in range(args.warmup):
                 b.run(params, mode, max_iters=S)
             dist.barrier()
@@ -825,14 +826,14 @@ def run_batch(args, dist: Dist, emit: bool = True):
             T = dist.reduce(time.perf_counter() - t, "max")
             arms[name] = dict(T=T, cands=dist.reduce(float(cands), "sum"), cells=dist.reduce(float(cells), "sum"),
                               clk=clocks.stop(), out=(cls, ids))
-    same = all(np.array_equal(a, c) for o in ("plain", "loops")
+    same = all(np.array_equal(a, c) for o in ("plain", "loops", "rounds")
                for a, c in zip(arms["batch"]["out"][0] + arms["batch"]["out"][1],
                                arms[o]["out"][0] + arms[o]["out"][1]))
     for db in dbs:
         db.close()
     if dist.rank != 0:
         return
-    bat, pln, lps = arms["batch"], arms["plain"], arms["loops"]
+    bat, pln, lps, rds = arms["batch"], arms["plain"], arms["loops"], arms["rounds"]
     n_dna = sum(1 for db in dbs if db.type == 0)
     out = {"metric": METRIC, "value": bat["cands"] / bat["T"], "unit": UNIT, "n_gpus": dist.world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * bat["T"] / args.steps,
@@ -854,6 +855,10 @@ def run_batch(args, dist: Dist, emit: bool = True):
            "loops": {"value": lps["cands"] / lps["T"], "ms_per_step": 1e3 * lps["T"] / args.steps,
                      "gcups": lps["cells"] / lps["T"] / 1e9,
                      "form": "one graph launch holding one conditional loop per job (NGIA_MODE_GRAPH)"},
+           "rounds": {"value": rds["cands"] / rds["T"], "ms_per_step": 1e3 * rds["T"] / args.steps,
+                      "gcups": rds["cells"] / rds["T"] / 1e9, "speedup_vs_plain": pln["T"] / rds["T"],
+                      "form": "every job's speculative-round driver on host worker threads, one stream per job "
+                              "(NGIA_MODE_SPEC)"},
            "speedup_vs_plain": pln["T"] / bat["T"], "speedup_vs_loops": lps["T"] / bat["T"],
            "bit_exact_vs_plain": bool(same),
            "clocks": bat["clk"], "plain_clocks": pln["clk"]}

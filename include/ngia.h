@@ -233,6 +233,10 @@ int ngia_batch_open(const ngia_db_view *jobs, int32_t n_jobs, ngia_batch **out);
  * records of net length < 16 while precise is 0 keeps its own while node
  * (the reference's word kernel then depends on job positions, func.cu:375);
  * at most 8,192 jobs of one record type (NGIA_E_LIMIT beyond);
+ * NGIA_MODE_SPEC: every job's speculative-round driver (as ngia_cluster in
+ * that mode), the jobs taken in turn by host worker threads
+ * (NGIA_BATCH_WORKERS, default 16), each job on its own stream, so one
+ * job's host round trips overlap the other jobs' GPU work;
  * NGIA_MODE_PLAIN: the jobs one after the other with the host-loop driver.
  * No reference counterpart (the reference clusters one database per run,
  * cluster.cpp:4-17).

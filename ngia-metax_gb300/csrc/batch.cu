@@ -7,15 +7,21 @@
 // job's greedy iteration (prepare, filter into the length classes, align
 // every class, next representative) re-run until the job is done.  Jobs run
 // concurrently with no host round trip per representative anywhere in the
-// batch, and the graph is captured once per parameter set.  The plain form
-// runs the jobs one after the other with the host-loop driver (the
-// reference's way of working, one job per run).  Every job's result is
-// identical to clustering it alone.
+// batch, and the graph is captured once per parameter set.  The pooled form
+// (pool.cu) runs the jobs of a record type in shared rounds; the speculative
+// form runs every job's speculative-round driver on host worker threads,
+// each job on its own stream.  The plain form runs the jobs one after the
+// other with the host-loop driver (the reference's way of working, one job
+// per run).  Every job's result is identical to clustering it alone.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <atomic>
+#include <mutex>
 #include <new>
+#include <string>
+#include <thread>
 #include <vector>
 
 #include "../host/host_common.h"
@@ -118,6 +124,51 @@ void destroy_pool_graph(ngia_batch *b) {
   b->pooled.clear();
   b->pprm.clear();
   b->ptune.clear();
+}
+
+// Host worker threads of the speculative batch form (NGIA_BATCH_WORKERS,
+// default 16); every worker takes the next job, clusters it with the
+// speculative driver, and repeats.  The first failure is reported (status
+// and message) once every worker has stopped.
+int run_spec_workers(ngia_batch *b, const ngia_params *params, int64_t max_iters) {
+  const size_t nj = b->jobs.size();
+  int workers = 16;
+  if (const char *w = getenv("NGIA_BATCH_WORKERS")) workers = std::max(1, std::min(256, atoi(w)));
+  workers = (int)std::min<size_t>((size_t)workers, nj);
+  std::atomic<size_t> next{0};
+  std::mutex mu;
+  int first_rc = NGIA_OK;
+  std::string first_msg;
+  auto work = [&]() {
+    for (;;) {
+      const size_t j = next.fetch_add(1);
+      if (j >= nj) return;
+      ngia_ctx *c = b->jobs[j];
+      int rc = cudaSetDevice(c->device) == cudaSuccess ? NGIA_OK : fail(NGIA_E_CUDA, "batch: cudaSetDevice");
+      if (!rc) {
+        c->tuned_warp_pairs = -1;
+        rc = ngia_cluster_begin(c, &params[j], NGIA_MODE_SPEC);
+      }
+      int32_t done = 0;
+      if (!rc) rc = ngia_cluster_step(c, max_iters, &done);
+      if (rc) {
+        char buf[512];
+        ngia_last_error(buf, sizeof(buf));
+        std::lock_guard<std::mutex> lock(mu);
+        if (first_rc == NGIA_OK) {
+          first_rc = rc;
+          first_msg = std::string("batch job ") + std::to_string(j) + ": " + buf;
+        }
+        next.store(nj);  // the others stop after their current job
+        return;
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 0; t < workers; t++) pool.emplace_back(work);
+  for (auto &t : pool) t.join();
+  if (first_rc != NGIA_OK) return fail(first_rc, "%s", first_msg.c_str());
+  return NGIA_OK;
 }
 
 bool batch_warp() {
@@ -240,7 +291,7 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
                               int32_t **cluster_out, int32_t **identity_out, ngia_stats *stats) {
   ngia::clear_error();
   if (!b || !params) return fail(NGIA_E_ARG, "ngia_batch_run: bad argument");
-  if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH && mode != NGIA_MODE_POOL)
+  if (mode != NGIA_MODE_PLAIN && mode != NGIA_MODE_GRAPH && mode != NGIA_MODE_POOL && mode != NGIA_MODE_SPEC)
     return fail(NGIA_E_ARG, "unknown mode %d", mode);
   const size_t nj = b->jobs.size();
   if (mode == NGIA_MODE_PLAIN) {
@@ -254,6 +305,12 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
       rc = ngia_cluster_step(c, max_iters, &done);
       if (rc) return rc;
     }
+  } else if (mode == NGIA_MODE_SPEC) {
+    // every job's speculative-round driver, the jobs taken in turn by host
+    // worker threads: each job runs on its own stream, so one job's round
+    // trips overlap the others' GPU work
+    int rc = run_spec_workers(b, params, max_iters);
+    if (rc) return rc;
   } else if (mode == NGIA_MODE_POOL) {
     // every job is set up on its own stream; the pools' tables are refreshed
     // with the jobs' run buffers and parameters; one launch runs the batch

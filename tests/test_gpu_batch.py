@@ -1,7 +1,8 @@
 """GPU: a batch of independent jobs (mixed DNA / protein, sizes and
 similarities) clustered in one CUDA graph launch (a loop per job, or the
-pooled rounds shared by the jobs of a record type), and one after the other
-with the plain driver, gives every job exactly the oracle's clustering."""
+pooled rounds shared by the jobs of a record type), with every job's
+speculative driver on host worker threads, and one after the other with the
+plain driver, gives every job exactly the oracle's clustering."""
 from __future__ import annotations
 
 import numpy as np
@@ -25,7 +26,7 @@ def _jobs():
     return dbs, params
 
 
-@pytest.mark.parametrize("mode", [ngia.MODE_GRAPH, ngia.MODE_POOL, ngia.MODE_PLAIN])
+@pytest.mark.parametrize("mode", [ngia.MODE_GRAPH, ngia.MODE_POOL, ngia.MODE_SPEC, ngia.MODE_PLAIN])
 def test_batch_matches_oracle_per_job(cuda_device, mode):
     dbs, params = _jobs()
     with ngia.Batch(dbs) as b:
@@ -43,7 +44,8 @@ def test_batch_sampled_iterations_agree(cuda_device):
     with ngia.Batch(dbs) as b:
         g = b.run(params, ngia.MODE_GRAPH, max_iters=5)
         q = b.run(params, ngia.MODE_POOL, max_iters=5)
+        r = b.run(params, ngia.MODE_SPEC, max_iters=5)
         p = b.run(params, ngia.MODE_PLAIN, max_iters=5)
-    for a, c, d in zip(g[0], p[0], q[0]):
-        assert np.array_equal(a, c) and np.array_equal(a, d)
-    assert g[2]["iterations"] == p[2]["iterations"] == q[2]["iterations"] == 5 * len(dbs)
+    for a, c, d, e in zip(g[0], p[0], q[0], r[0]):
+        assert np.array_equal(a, c) and np.array_equal(a, d) and np.array_equal(a, e)
+    assert g[2]["iterations"] == p[2]["iterations"] == q[2]["iterations"] == r[2]["iterations"] == 5 * len(dbs)

@@ -79,3 +79,13 @@ def test_pool_sampled_iterations(cuda_device):
     with ngia.Batch(dbs) as b:
         cls, ids, st = b.run(params, ngia.MODE_POOL, max_iters=7)
     _check(dbs, params, cls, ids, st, max_iters=7)
+
+
+def test_speculative_batch_matches_oracle_on_mixed_jobs(cuda_device, monkeypatch):
+    """The speculative batch form on the same jobs, with fewer worker threads
+    than jobs (each worker clusters several jobs in turn)."""
+    monkeypatch.setenv("NGIA_BATCH_WORKERS", "3")
+    dbs, params = _mixed()
+    with ngia.Batch(dbs) as b:
+        cls, ids, st = b.run(params, ngia.MODE_SPEC)
+    _check(dbs, params, cls, ids, st)
