@@ -477,8 +477,7 @@ int spec_prepare(ngia_ctx *c) {
   if (const char *b = getenv("NGIA_SPEC_BUDGET")) sp->budget = std::max(1, std::min(kSpecBudget, atoi(b)));
   sp->max_alive = kSpecMaxAlive;
   if (const char *m = getenv("NGIA_SPEC_MAX_ALIVE")) sp->max_alive = std::max(2, atoi(m));
-  // iterations over larger sets run in the captured loop
-  return ensure_graph(c);
+  return NGIA_OK;
 }
 
 void spec_free(ngia_ctx *c) {
@@ -522,6 +521,10 @@ int spec_step(ngia_ctx *c, int64_t max_iters) {
       // at the unclustered set
       const int64_t room = limit - c->h_state->iter;
       const int64_t n_it = exact ? std::min<int64_t>(room, kSpecRecheck) : room;
+      // captured on first use (databases that start below the threshold,
+      // such as serving leftovers, never need it)
+      int rc0 = ensure_graph(c);
+      if (rc0) return rc0;
       c->h_state->iter_limit = c->h_state->iter + n_it;
       CKP(cudaMemcpyAsync(&c->rb.st->iter_limit, &c->h_state->iter_limit, sizeof(int64_t), cudaMemcpyHostToDevice,
                           c->stream));
