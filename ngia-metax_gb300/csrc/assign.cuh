@@ -177,6 +177,16 @@ __global__ void __launch_bounds__(256) k_serve_filter(DevDB qdb, RepStore rs, Ru
 #ifndef NGIA_SERVE_STAGE
 #define NGIA_SERVE_STAGE 0
 #endif
+// NGIA_SERVE_FMA (DNA, without staging): the per-column bookkeeping on the FMA
+// pipe with the table in global memory; NGIA_SERVE_REM_ROUND: remainder tiles
+// rounded up to a multiple of this width (fewer tile bodies: the warps of
+// these kernels see many window widths).
+#ifndef NGIA_SERVE_FMA
+#define NGIA_SERVE_FMA 0
+#endif
+#ifndef NGIA_SERVE_REM_ROUND
+#define NGIA_SERVE_REM_ROUND 1
+#endif
 
 // Banded LCS of the queued (representative, query) pairs of one class: the
 // loop of k_align_tiled (align.cu) with the representative taken per pair.
@@ -359,6 +369,26 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
         ncw = 0;
       }
       if (rem > 0) zw += tiled_rem_eqf<Ring, MT>(rem, ring, w_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+    } else if constexpr (P == 2 && NGIA_SERVE_EQ && NGIA_SERVE_FMA) {
+      // match words from the pair's representative's table (global memory,
+      // L1), the per-column bookkeeping on the FMA pipe as in k_align_tiled
+      const uint64_t req = (uint64_t)(rs.eq + (int64_t)r * rs.eq_stride);
+      uint32_t wc[2];
+      eq_codes_top(cur, wc);
+      uint32_t cw = 0, ncw = 0;
+      int base = js;
+      zw = 0;  // the tiles return their rows' zero counts
+      for (int t = 0; t < full; t++, base += MT) {
+        zw += tiled_tile_eqfg<MT, NGIA_SERVE_PF, Ring>(ring, req, base, je, nb1, cols, wc, cw, ncw, fk);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      for (; rem >= MT; rem -= MT, base += MT) {
+        zw += tiled_tile_eqfg<MT, NGIA_SERVE_PF, Ring>(ring, req, base, je, nb1, cols, wc, cw, ncw, fk);
+        cw = ncw << (32 - cols);
+        ncw = 0;
+      }
+      if (rem > 0) zw += tiled_rem_eqfg<Ring, NGIA_SERVE_REM_ROUND>(rem, ring, req, base, je, nb1, cols, wc, cw, ncw, fk);
     } else if constexpr (P == 2 && NGIA_SERVE_EQ) {  // match words from the pair's representative's table
       const uint32_t *req = rs.eq + (int64_t)r * rs.eq_stride;
       uint32_t q4[4];

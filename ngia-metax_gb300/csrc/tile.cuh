@@ -438,6 +438,103 @@ __device__ __forceinline__ int tiled_rem_eqf(int rem, const Ring &ring, uint32_t
   }
 }
 
+// ---- the same bookkeeping with the match table in global memory ------------
+// (kernels that take the representative per pair read its table through L1)
+__device__ __forceinline__ uint64_t eq_next_addr_g(uint32_t &w, uint64_t eb, const FmaK &k) {
+  uint32_t c;
+  uint64_t a;
+  asm("mul.hi.u32 %0, %1, %2;" : "=r"(c) : "r"(w), "r"(k.four));
+  asm("mul.lo.u32 %0, %0, %1;" : "+r"(w) : "r"(k.four));
+  asm("mad.wide.u32 %0, %1, %2, %3;" : "=l"(a) : "r"(c), "r"(k.four), "l"(eb));
+  return a;
+}
+
+template <int M, int TW>
+struct EqLoadG {
+  static __device__ __forceinline__ void run(uint32_t (&e)[TW], uint64_t a) {
+    EqLoadG<M - 1, TW>::run(e, a);
+    asm volatile("ld.global.nc.u32 %0, [%1+%2];" : "=r"(e[M - 1]) : "l"(a), "n"(16 * (M - 1)));
+  }
+};
+template <int TW>
+struct EqLoadG<0, TW> {
+  static __device__ __forceinline__ void run(uint32_t (&)[TW], uint64_t) {}
+};
+
+template <int TW, bool CC, bool PF>
+__device__ __forceinline__ void eq_columns_fg(uint32_t (&row)[TW], uint64_t eb, const uint32_t (&wc)[2], int cols,
+                                              uint32_t &cw, uint32_t &ncw, const FmaK &k) {
+#pragma unroll 1
+  for (int h = 0; h < 2; h++) {
+    const int n = min(16, cols - 16 * h);
+    if (n <= 0) break;
+    uint32_t w = wc[h];
+    if constexpr (PF) {
+      uint32_t ea[TW], eo[TW];
+      EqLoadG<TW, TW>::run(ea, eq_next_addr_g(w, eb, k));
+      int c = 0;
+#pragma unroll 1
+      for (; c + 2 <= n; c += 2) {
+        EqLoadG<TW, TW>::run(eo, eq_next_addr_g(w, eb, k));
+        dp_tile_eqf<TW, CC, CC, NGIA_EQ_MADC>(row, ea, cw, ncw, k.one);
+        EqLoadG<TW, TW>::run(ea, eq_next_addr_g(w, eb, k));  // past the last column: code 0, in bounds
+        dp_tile_eqf<TW, CC, CC, NGIA_EQ_MADC>(row, eo, cw, ncw, k.one);
+      }
+      if (c < n) dp_tile_eqf<TW, CC, CC, NGIA_EQ_MADC>(row, ea, cw, ncw, k.one);
+    } else {
+#pragma unroll 1
+      for (int c = 0; c < n; c++) {
+        uint32_t ev[TW];
+        EqLoadG<TW, TW>::run(ev, eq_next_addr_g(w, eb, k));
+        dp_tile_eqf<TW, CC, CC, NGIA_EQ_MADC>(row, ev, cw, ncw, k.one);
+      }
+    }
+  }
+}
+
+// tiled_tile_eqf with the table at global address eqb; returns the zero
+// count of the tile's rows after the block.
+template <int TW, bool PF, class Ring>
+__device__ __forceinline__ int tiled_tile_eqfg(const Ring &ring, uint64_t eqb, int base, int je, int nb1, int cols,
+                                               const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw, const FmaK &k) {
+  uint32_t row[TW];
+#pragma unroll
+  for (int m = 0; m < TW; m++) {
+    const int j = base + m;
+    row[m] = j <= je ? ring[j] : 0u;
+  }
+  eq_columns_fg<TW, true, PF>(row, eqb + 16ull * (uint64_t)min(base, nb1), wc, cols, cw, ncw, k);
+  int znew = 0;
+#pragma unroll
+  for (int m = 0; m < TW; m++) {
+    const int j = base + m;
+    if (j <= je) {
+      ring[j] = row[m];
+      znew += __popc(~row[m]);
+    }
+  }
+  return znew;
+}
+
+// The last tile of a block row: `rem` slots rounded up to a multiple of R
+// (1..32; fewer tile bodies for kernels whose warps see many window widths).
+template <class Ring, int R>
+__device__ __forceinline__ int tiled_rem_eqfg(int rem, const Ring &ring, uint64_t eqb, int base, int je, int nb1,
+                                              int cols, const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw,
+                                              const FmaK &k) {
+  switch ((rem + R - 1) / R * R) {
+#define NGIA_REMG(W) \
+  case W:            \
+    if (W % R == 0) return tiled_tile_eqfg<W % R == 0 ? W : 1, false, Ring>(ring, eqb, base, je, nb1, cols, wc, cw, ncw, k); \
+    return 0;
+    NGIA_REMG(1) NGIA_REMG(2) NGIA_REMG(3) NGIA_REMG(4) NGIA_REMG(5) NGIA_REMG(6) NGIA_REMG(7) NGIA_REMG(8)
+    NGIA_REMG(9) NGIA_REMG(10) NGIA_REMG(11) NGIA_REMG(12) NGIA_REMG(13) NGIA_REMG(14) NGIA_REMG(15) NGIA_REMG(16)
+#undef NGIA_REMG
+    default:
+      return 0;
+  }
+}
+
 constexpr int kEqRemRound = NGIA_EQ_REM_ROUND;  // remainder tile widths: multiples of this
 
 template <class Ring, int MT>
