@@ -178,11 +178,14 @@ __global__ void __launch_bounds__(256) k_serve_filter(DevDB qdb, RepStore rs, Ru
 #define NGIA_SERVE_STAGE 0
 #endif
 // NGIA_SERVE_FMA (DNA, without staging): the per-column bookkeeping on the FMA
-// pipe with the table in global memory; NGIA_SERVE_REM_ROUND: remainder tiles
-// rounded up to a multiple of this width (fewer tile bodies: the warps of
-// these kernels see many window widths).
+// pipe with the table in global memory (as k_align_tiled does with its
+// shared-memory table).  Measured on GB300: serving 64.3k against 58.9k
+// queries/s (configuration 5, p99 642 against 782 ms), the speculative rounds
+// of the 20,000-sequence job 0.489 against 0.506 s.
+// NGIA_SERVE_REM_ROUND: remainder tiles rounded up to a multiple of this width
+// (fewer tile bodies); 2, 4 and 8 gave 63.5k, 62.2k and 59.1k queries/s.
 #ifndef NGIA_SERVE_FMA
-#define NGIA_SERVE_FMA 0
+#define NGIA_SERVE_FMA 1
 #endif
 #ifndef NGIA_SERVE_REM_ROUND
 #define NGIA_SERVE_REM_ROUND 1
