@@ -12,7 +12,9 @@
 //  NGIA_TILED_MAIN_DNA / NGIA_TILED_BLOCKS_DNA  main tile width and resident
 //    CTAs per SM of the tiled kernel: 16 slots at 4 CTAs.  24 and 32 slots,
 //    and 5 CTAs, were slower (the kernel is sensitive to its instruction
-//    footprint: wider tiles mean larger unrolled bodies).
+//    footprint: wider tiles mean larger unrolled bodies).  With the FMA-pipe
+//    bookkeeping: 4 CTAs 0.723 of the INT32 bound, 5 CTAs (95 registers)
+//    0.685, the main tiles without prefetch 0.691, both 0.669.
 //  NGIA_ALIGN_EQ / NGIA_WIN_EQ  match words from the representative's match
 //    table (1) instead of from plane registers (0): 16% (tiled, s=0.85) and
 //    12-26% (window kernels, s=0.9-0.95) more candidate seqs/s.
