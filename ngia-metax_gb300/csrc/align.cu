@@ -215,6 +215,10 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
   const float s = prm.s;
   const int nb1 = h.nb1;
   const uint32_t vlast = (h.net1 & 31) ? ((1u << (h.net1 & 31)) - 1u) : 0xFFFFFFFFu;
+  // 1 and 4 as values ptxas cannot fold (nb1 is read from shared memory)
+  const uint32_t one_rt = 1u + (uint32_t)(h.nb1 < 0);
+  const FmaK fk{one_rt, one_rt << 2};
+  (void)fk;
 
   uint32_t row[WC], pl[kEq ? 1 : P][WC], cur[P], nxt[P];
   int state = -1, entry = 0, cand = 0;
@@ -275,10 +279,17 @@ __global__ void __launch_bounds__(kAlignThreads, win_min_blocks(P, WC))
       // match words of slot m for column k: s_eq[4 (js + m) + code_k]; slots
       // past je read blocks not in the band (or the table's zero blocks):
       // those rows are reset when they enter the band
-      uint32_t q[4];
-      eq_codes(cur, q);
-      const char *eb = reinterpret_cast<const char *>(s_eq + 4 * js);
-      eq_columns<WC, false, NGIA_EQ_PF_WIN>(row, eb, q, cols, cw_unused, cw_unused);
+      if constexpr (NGIA_WIN_FMA) {  // the per-column bookkeeping on the FMA pipe (tile.cuh)
+        uint32_t wc[2];
+        eq_codes_top(cur, wc);
+        eq_columns_f<WC, false, NGIA_EQ_PF_WIN>(row, smem_u32(s_eq) + 16u * (uint32_t)js, wc, cols, cw_unused,
+                                                 cw_unused, fk);
+      } else {
+        uint32_t q[4];
+        eq_codes(cur, q);
+        const char *eb = reinterpret_cast<const char *>(s_eq + 4 * js);
+        eq_columns<WC, false, NGIA_EQ_PF_WIN>(row, eb, q, cols, cw_unused, cw_unused);
+      }
     } else {
     uint32_t rv[P];
 #pragma unroll

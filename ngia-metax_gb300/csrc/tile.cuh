@@ -98,6 +98,12 @@
 //    16+16+16+1), the last main tile and that slot run as one tile of MT+1
 //    slots, saving a tile's per-column overhead.  Off: 0.99x on GB300
 //    (7.15 vs 7.07 ms per launch, 1M DNA s=0.85).
+//  NGIA_WIN_FMA  1: the register-window kernels take each column's code and
+//    the match words' address as multiply-adds on the FMA pipe, as the tiled
+//    kernel does.
+#ifndef NGIA_WIN_FMA
+#define NGIA_WIN_FMA 0
+#endif
 #ifndef NGIA_TILED_MERGE1
 #define NGIA_TILED_MERGE1 0
 #endif
