@@ -100,7 +100,9 @@
 //    (7.15 vs 7.07 ms per launch, 1M DNA s=0.85).
 //  NGIA_WIN_FMA  1: the register-window kernels take each column's code and
 //    the match words' address as multiply-adds on the FMA pipe, as the tiled
-//    kernel does.
+//    kernel does.  Off: no difference on GB300 (the 32-block class of 1M DNA
+//    0.444 ms per iteration either way, the 20,000-sequence job's graph
+//    form 2.93-3.00 s): these classes' launches are bound by latency.
 #ifndef NGIA_WIN_FMA
 #define NGIA_WIN_FMA 0
 #endif
