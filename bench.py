@@ -55,6 +55,8 @@ def parse():
                     help="dna_small | dna_1m | protein_200k | batch256 | serve | dna_1m_whole")
     ap.add_argument("--batch-jobs", type=int, default=256)
     ap.add_argument("--batch-max-seqs", type=int, default=200000)
+    ap.add_argument("--batch-autotune", type=int, default=0,
+                    help="batch workloads: ngia_batch_autotune with this many iterations per setting first (0: off)")
     ap.add_argument("--batch-iters", type=int, default=-1,
                     help="batch256: greedy iterations per job and step (-1: --iters-per-step, 0: whole jobs)")
     ap.add_argument("--serve-batches", type=int, default=200)
@@ -809,7 +811,16 @@ def run_batch(args, dist: Dist, emit: bool = True):
     dbs, params = [j[0] for j in jobs], [j[1] for j in jobs]
     n_total = sum(db.n for db in dbs)
     arms = {}
+    tuning = None
     with ngia.Batch(dbs) as b:
+        if args.batch_autotune > 0:
+            t0 = time.perf_counter()
+            tun = b.autotune(params, args.batch_autotune)
+            tuning = {"iters_per_setting": args.batch_autotune, "seconds": round(time.perf_counter() - t0, 2),
+                      "jobs": len(tun), "cached": int(sum(t["cached"] for t in tun)),
+                      "non_default": int(sum(1 for t in tun if t["word_order"] or t["refill"] != 32 or
+                                             t["warp_pairs"] != -1 or any(x != -1 for x in t["class_warp_pairs"]) or
+                                             any(x != 1 for x in t["class_grid_div"]) or t["filter_tile"] != 8))}
         for mode, name in ((ngia.MODE_POOL, "batch"), (ngia.MODE_GRAPH, "loops"), (ngia.MODE_SPEC, "rounds"),
                            (ngia.MODE_PLAIN, "plain")):
             for _ in range(args.warmup):
@@ -860,7 +871,7 @@ def run_batch(args, dist: Dist, emit: bool = True):
                       "form": "every job's speculative-round driver on host worker threads, one stream per job "
                               "(NGIA_MODE_SPEC)"},
            "speedup_vs_plain": pln["T"] / bat["T"], "speedup_vs_loops": lps["T"] / bat["T"],
-           "bit_exact_vs_plain": bool(same),
+           "bit_exact_vs_plain": bool(same), "batch_tuning": tuning,
            "clocks": bat["clk"], "plain_clocks": pln["clk"]}
     if emit:
         print(json.dumps(out), flush=True)

@@ -416,6 +416,16 @@ typedef struct ngia_tuning {
 int ngia_autotune(ngia_ctx *ctx, const ngia_params *p, int32_t iters, ngia_tuning *out);
 int ngia_set_tuning(ngia_ctx *ctx, const ngia_tuning *t);
 
+/* Tunes every job of the batch with ngia_autotune (its first `iters` greedy
+ * iterations per candidate setting: test order, refill, and per length
+ * bucket the warp-per-pair cut-off, the CTA count and the composition
+ * filter's tile; jobs whose database shape and parameters were tuned before
+ * in the process take the cached settings without timing) and reports each
+ * job's settings in out[j] (may be NULL).  Later NGIA_MODE_GRAPH runs keep
+ * every tuned job's settings instead of running all its buckets thread per
+ * pair.  Results never change.  No reference counterpart. */
+int ngia_batch_autotune(ngia_batch *b, const ngia_params *params, int32_t iters, ngia_tuning *out);
+
 /* Loads another database into an open context, reusing its device memory
  * (one host-to-device copy of the records and offsets, then the header
  * arrays are rebuilt on the device).  The database must fit what the context

@@ -55,6 +55,7 @@ struct ngia_batch {
   std::vector<ngia::RunParams> pprm;      // parameters of the own-node jobs at capture
   std::vector<int> ptune;                 // their tuning generation at capture
   cudaStream_t pstream = nullptr;         // capture and launch stream of the pooled graph
+  std::vector<int> tuned;                 // per job: 1 after ngia_batch_autotune
 };
 
 namespace {
@@ -352,7 +353,8 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
       // NGIA_BATCH_WARP=1 keeps each job's own warp-per-pair cut-off:
       // 17.97M against 20.97M over the first 8 iterations, 4.23 against
       // 4.31 s for 256 small jobs clustered to the end
-      c->tuned_warp_pairs = batch_warp() ? -1 : 0;
+      // a job tuned by ngia_batch_autotune keeps its own settings
+      if (b->tuned.size() != nj || !b->tuned[j]) c->tuned_warp_pairs = batch_warp() ? -1 : 0;
       int rc = ngia_cluster_begin(c, &params[j], NGIA_MODE_PLAIN);  // no per-job graph
       if (rc) return rc;
       c->mode = NGIA_MODE_GRAPH;
@@ -394,6 +396,20 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
     sum.done_cells += s.done_cells;
   }
   if (stats) *stats = sum;
+  return NGIA_OK;
+}
+
+extern "C" int ngia_batch_autotune(ngia_batch *b, const ngia_params *params, int32_t iters, ngia_tuning *out) {
+  ngia::clear_error();
+  if (!b || !params || iters <= 0) return fail(NGIA_E_ARG, "ngia_batch_autotune: bad argument");
+  b->tuned.assign(b->jobs.size(), 0);
+  for (size_t j = 0; j < b->jobs.size(); j++) {
+    ngia_tuning t;
+    int rc = ngia_autotune(b->jobs[j], &params[j], iters, &t);  // cached by database shape and parameters
+    if (rc) return rc;
+    if (out) out[j] = t;
+    b->tuned[j] = 1;
+  }
   return NGIA_OK;
 }
 

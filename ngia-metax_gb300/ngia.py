@@ -125,6 +125,7 @@ def lib() -> C.CDLL:
         "ngia_batch_open": (C.c_int, [P(DBView), I32, P(VP)]),
         "ngia_batch_run": (C.c_int, [VP, P(Params), I32, I64, P(P(I32)), P(P(I32)), P(Stats)]),
         "ngia_batch_close": (C.c_int, [VP]),
+        "ngia_batch_autotune": (C.c_int, [VP, P(Params), I32, P(Tuning)]),
         "ngia_serve_open": (C.c_int, [P(DBView), P(Params), P(ServeConfig), P(VP)]),
         "ngia_serve_slots": (C.c_int, [VP, P(I32)]),
         "ngia_serve_submit": (C.c_int, [VP, P(DBView), P(I64)]),
@@ -590,6 +591,15 @@ class Batch:
         st = Stats()
         _check(lib().ngia_batch_run(self._h, ps, mode, max_iters, cptr, iptr, C.byref(st)))
         return cls, ids, st.as_dict()
+
+    def autotune(self, params: list, iters: int = 4) -> list:
+        """Tunes every job (cached by database shape); returns each job's settings."""
+        n = len(self.dbs)
+        ps = (Params * n)(*params)
+        ts = (Tuning * n)()
+        _check(lib().ngia_batch_autotune(self._h, ps, iters, ts))
+        return [{f: (list(getattr(t, f)) if f.startswith("class_") else getattr(t, f)) for f, _ in Tuning._fields_}
+                for t in ts]
 
     def close(self) -> None:
         if self._h:

@@ -49,3 +49,18 @@ def test_batch_sampled_iterations_agree(cuda_device):
     for a, c, d, e in zip(g[0], p[0], q[0], r[0]):
         assert np.array_equal(a, c) and np.array_equal(a, d) and np.array_equal(a, e)
     assert g[2]["iterations"] == p[2]["iterations"] == q[2]["iterations"] == r[2]["iterations"] == 5 * len(dbs)
+
+
+def test_batch_autotune_keeps_results(cuda_device):
+    """Every job tuned (per length bucket: warp-per-pair cut-off, CTA count,
+    filter tile; jobs of one shape share the cached settings), then the
+    one-loop-per-job form with the tuned settings: still the oracle's
+    clustering per job."""
+    dbs, params = _jobs()
+    with ngia.Batch(dbs) as b:
+        tun = b.autotune(params, 2)
+        assert len(tun) == len(dbs) and all(t["refill"] >= 1 for t in tun)
+        cls, ids, st = b.run(params, ngia.MODE_GRAPH)
+    for db, p, cl, ident in zip(dbs, params, cls, ids):
+        ocl, oid, _ = oracle.cluster(db.words, db.rec_off, db.type, p.similarity, p.word_length, p.precise)
+        assert np.array_equal(cl, ocl) and np.array_equal(ident, oid)
