@@ -818,9 +818,9 @@ def run_batch(args, dist: Dist, emit: bool = True):
             tun = b.autotune(params, args.batch_autotune)
             tuning = {"iters_per_setting": args.batch_autotune, "seconds": round(time.perf_counter() - t0, 2),
                       "jobs": len(tun), "cached": int(sum(t["cached"] for t in tun)),
-                      "non_default": int(sum(1 for t in tun if t["word_order"] or t["refill"] != 32 or
-                                             t["warp_pairs"] != -1 or any(x != -1 for x in t["class_warp_pairs"]) or
-                                             any(x != 1 for x in t["class_grid_div"]) or t["filter_tile"] != 8))}
+                      "policy": ["thread", "cutoff", "tuned"][b.policy()],
+                      "ms_per_iter": round(tun[0]["ms_per_iter"], 3),
+                      "thread_ms_per_iter": round(tun[0]["default_ms_per_iter"], 3)}
         for mode, name in ((ngia.MODE_POOL, "batch"), (ngia.MODE_GRAPH, "loops"), (ngia.MODE_SPEC, "rounds"),
                            (ngia.MODE_PLAIN, "plain")):
             for _ in range(args.warmup):

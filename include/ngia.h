@@ -416,15 +416,30 @@ typedef struct ngia_tuning {
 int ngia_autotune(ngia_ctx *ctx, const ngia_params *p, int32_t iters, ngia_tuning *out);
 int ngia_set_tuning(ngia_ctx *ctx, const ngia_tuning *t);
 
-/* Tunes every job of the batch with ngia_autotune (its first `iters` greedy
- * iterations per candidate setting: test order, refill, and per length
- * bucket the warp-per-pair cut-off, the CTA count and the composition
- * filter's tile; jobs whose database shape and parameters were tuned before
- * in the process take the cached settings without timing) and reports each
- * job's settings in out[j] (may be NULL).  Later NGIA_MODE_GRAPH runs keep
- * every tuned job's settings instead of running all its buckets thread per
- * pair.  Results never change.  No reference counterpart. */
+/* Chooses the settings the batch's NGIA_MODE_GRAPH runs (one greedy loop
+ * per job, side by side) give their jobs, by timing three policies on the
+ * whole batch over the first `iters` greedy iterations of every job:
+ *   NGIA_BATCH_POLICY_THREAD  every length bucket of every job aligned
+ *                             thread per pair (the untuned batch default);
+ *   NGIA_BATCH_POLICY_CUTOFF  each job's default warp-per-pair cut-off;
+ *   NGIA_BATCH_POLICY_TUNED   each job's own ngia_autotune settings, found
+ *                             with the job alone on the GPU (cached by
+ *                             database shape and parameters).
+ * The thread-per-pair policy stays unless another is at least 2% faster.
+ * Later NGIA_MODE_GRAPH runs apply the chosen policy; out[j] (may be NULL)
+ * receives job j's settings under it (candidates = 3, ms_per_iter and
+ * default_ms_per_iter the batch's wall time per iteration under the chosen
+ * and the thread-per-pair policy).  Results never change.  No reference
+ * counterpart. */
+#define NGIA_BATCH_POLICY_THREAD 0
+#define NGIA_BATCH_POLICY_CUTOFF 1
+#define NGIA_BATCH_POLICY_TUNED  2
 int ngia_batch_autotune(ngia_batch *b, const ngia_params *params, int32_t iters, ngia_tuning *out);
+/* Applies a policy without timing (NGIA_BATCH_POLICY_TUNED only after
+ * ngia_batch_autotune, NGIA_E_STATE before); ngia_batch_policy reports the
+ * policy in force (-1 before either call). */
+int ngia_batch_set_policy(ngia_batch *b, int32_t policy);
+int ngia_batch_policy(const ngia_batch *b, int32_t *policy);
 
 /* Loads another database into an open context, reusing its device memory
  * (one host-to-device copy of the records and offsets, then the header

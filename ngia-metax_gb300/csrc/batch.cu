@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <atomic>
+#include <chrono>
 #include <mutex>
 #include <new>
 #include <string>
@@ -55,7 +56,12 @@ struct ngia_batch {
   std::vector<ngia::RunParams> pprm;      // parameters of the own-node jobs at capture
   std::vector<int> ptune;                 // their tuning generation at capture
   cudaStream_t pstream = nullptr;         // capture and launch stream of the pooled graph
-  std::vector<int> tuned;                 // per job: 1 after ngia_batch_autotune
+  // the per-job-loop form's policy chosen by ngia_batch_autotune
+  // (NGIA_BATCH_POLICY_*; -1 before) and each job's warp-per-pair cut-off
+  // under it, restored on every NGIA_MODE_GRAPH run
+  int policy = -1;
+  std::vector<int> policy_wp;
+  std::vector<ngia_tuning> own;  // each job's own tuning (ngia_batch_autotune)
 };
 
 namespace {
@@ -353,8 +359,11 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
       // NGIA_BATCH_WARP=1 keeps each job's own warp-per-pair cut-off:
       // 17.97M against 20.97M over the first 8 iterations, 4.23 against
       // 4.31 s for 256 small jobs clustered to the end
-      // a job tuned by ngia_batch_autotune keeps its own settings
-      if (b->tuned.size() != nj || !b->tuned[j]) c->tuned_warp_pairs = batch_warp() ? -1 : 0;
+      // after ngia_batch_autotune, the chosen policy's settings
+      if (b->policy >= 0 && b->policy_wp.size() == nj)
+        c->tuned_warp_pairs = b->policy_wp[j];
+      else
+        c->tuned_warp_pairs = batch_warp() ? -1 : 0;
       int rc = ngia_cluster_begin(c, &params[j], NGIA_MODE_PLAIN);  // no per-job graph
       if (rc) return rc;
       c->mode = NGIA_MODE_GRAPH;
@@ -399,17 +408,100 @@ extern "C" int ngia_batch_run(ngia_batch *b, const ngia_params *params, int32_t 
   return NGIA_OK;
 }
 
+namespace {
+
+// The settings of one job under a batch policy: the untuned settings with
+// every bucket thread per pair, the untuned settings with the job's default
+// warp-per-pair cut-off, or the job's own tuning.
+ngia_tuning policy_setting(int policy, const ngia_tuning &own) {
+  if (policy == NGIA_BATCH_POLICY_TUNED) return own;
+  ngia_tuning t;
+  std::memset(&t, 0, sizeof(t));
+  t.word_order = 0;
+  t.refill = 32;
+  t.warp_pairs = policy == NGIA_BATCH_POLICY_THREAD ? 0 : -1;
+  for (int k = 0; k < 8; k++) {
+    t.class_warp_pairs[k] = -1;
+    t.class_grid_div[k] = 1;
+  }
+  t.filter_tile = 8;
+  return t;
+}
+
+int apply_policy(ngia_batch *b, int policy, const std::vector<ngia_tuning> &own) {
+  b->policy = policy;
+  b->policy_wp.assign(b->jobs.size(), 0);
+  for (size_t j = 0; j < b->jobs.size(); j++) {
+    const ngia_tuning t = policy_setting(policy, own[j]);
+    int rc = ngia_set_tuning(b->jobs[j], &t);
+    if (rc) return rc;
+    b->policy_wp[j] = t.warp_pairs;
+  }
+  return NGIA_OK;
+}
+
+}  // namespace
+
 extern "C" int ngia_batch_autotune(ngia_batch *b, const ngia_params *params, int32_t iters, ngia_tuning *out) {
   ngia::clear_error();
   if (!b || !params || iters <= 0) return fail(NGIA_E_ARG, "ngia_batch_autotune: bad argument");
-  b->tuned.assign(b->jobs.size(), 0);
-  for (size_t j = 0; j < b->jobs.size(); j++) {
-    ngia_tuning t;
-    int rc = ngia_autotune(b->jobs[j], &params[j], iters, &t);  // cached by database shape and parameters
+  const size_t nj = b->jobs.size();
+  // every job's own tuning, found alone (cached by database shape)
+  b->own.assign(nj, ngia_tuning{});
+  std::vector<ngia_tuning> &own = b->own;
+  for (size_t j = 0; j < nj; j++) {
+    int rc = ngia_autotune(b->jobs[j], &params[j], iters, &own[j]);
     if (rc) return rc;
-    if (out) out[j] = t;
-    b->tuned[j] = 1;
   }
+  // each policy timed on the whole batch, the first `iters` iterations of
+  // every job in one graph launch: one untimed launch (graph capture), then
+  // the faster of two
+  const int policies[3] = {NGIA_BATCH_POLICY_THREAD, NGIA_BATCH_POLICY_CUTOFF, NGIA_BATCH_POLICY_TUNED};
+  double ms[3];
+  for (int q = 0; q < 3; q++) {
+    int rc = apply_policy(b, policies[q], own);
+    if (rc) return rc;
+    ms[q] = 1e300;
+    for (int r = 0; r < 3; r++) {
+      const auto t0 = std::chrono::steady_clock::now();
+      rc = ngia_batch_run(b, params, NGIA_MODE_GRAPH, iters, nullptr, nullptr, nullptr);
+      if (rc) return rc;
+      const double t = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+      if (r > 0) ms[q] = std::min(ms[q], t);
+    }
+  }
+  // the thread-per-pair policy stays unless another is 2% faster (the
+  // timings of one policy differ by about 1% between launches)
+  int best = 0;
+  for (int q = 1; q < 3; q++)
+    if (ms[q] < ms[best] * 0.98) best = q;
+  int rc = apply_policy(b, policies[best], own);
+  if (rc) return rc;
+  if (out)
+    for (size_t j = 0; j < nj; j++) {
+      out[j] = policy_setting(policies[best], own[j]);
+      out[j].candidates = 3;
+      out[j].ms_per_iter = ms[best] / iters;
+      out[j].default_ms_per_iter = ms[0] / iters;
+      out[j].cached = own[j].cached;
+    }
+  return NGIA_OK;
+}
+
+extern "C" int ngia_batch_set_policy(ngia_batch *b, int32_t policy) {
+  ngia::clear_error();
+  if (!b || policy < NGIA_BATCH_POLICY_THREAD || policy > NGIA_BATCH_POLICY_TUNED)
+    return fail(NGIA_E_ARG, "ngia_batch_set_policy: bad argument");
+  if (policy == NGIA_BATCH_POLICY_TUNED && b->own.size() != b->jobs.size())
+    return fail(NGIA_E_STATE, "ngia_batch_set_policy: the jobs' own settings come from ngia_batch_autotune");
+  if (b->own.size() != b->jobs.size()) b->own.assign(b->jobs.size(), ngia_tuning{});
+  return apply_policy(b, policy, b->own);
+}
+
+extern "C" int ngia_batch_policy(const ngia_batch *b, int32_t *policy) {
+  ngia::clear_error();
+  if (!b || !policy) return fail(NGIA_E_ARG, "ngia_batch_policy: bad argument");
+  *policy = b->policy;
   return NGIA_OK;
 }
 

@@ -19,6 +19,7 @@ MODE_PLAIN = 0
 MODE_GRAPH = 1
 MODE_SPEC = 2
 MODE_POOL = 3  # batches only: the jobs of one record type share every launch
+POLICY_THREAD, POLICY_CUTOFF, POLICY_TUNED = 0, 1, 2  # batch policies of MODE_GRAPH runs
 
 
 class NgiaError(RuntimeError):
@@ -126,6 +127,8 @@ def lib() -> C.CDLL:
         "ngia_batch_run": (C.c_int, [VP, P(Params), I32, I64, P(P(I32)), P(P(I32)), P(Stats)]),
         "ngia_batch_close": (C.c_int, [VP]),
         "ngia_batch_autotune": (C.c_int, [VP, P(Params), I32, P(Tuning)]),
+        "ngia_batch_set_policy": (C.c_int, [VP, I32]),
+        "ngia_batch_policy": (C.c_int, [VP, P(I32)]),
         "ngia_serve_open": (C.c_int, [P(DBView), P(Params), P(ServeConfig), P(VP)]),
         "ngia_serve_slots": (C.c_int, [VP, P(I32)]),
         "ngia_serve_submit": (C.c_int, [VP, P(DBView), P(I64)]),
@@ -593,13 +596,25 @@ class Batch:
         return cls, ids, st.as_dict()
 
     def autotune(self, params: list, iters: int = 4) -> list:
-        """Tunes every job (cached by database shape); returns each job's settings."""
+        """Times the three batch policies (thread per pair, default cut-off,
+        each job's own tuning) and keeps the fastest; returns each job's
+        settings under it."""
         n = len(self.dbs)
         ps = (Params * n)(*params)
         ts = (Tuning * n)()
         _check(lib().ngia_batch_autotune(self._h, ps, iters, ts))
         return [{f: (list(getattr(t, f)) if f.startswith("class_") else getattr(t, f)) for f, _ in Tuning._fields_}
                 for t in ts]
+
+    def set_policy(self, policy: int) -> None:
+        """Applies a batch policy (POLICY_*) to later MODE_GRAPH runs."""
+        _check(lib().ngia_batch_set_policy(self._h, policy))
+
+    def policy(self) -> int:
+        """The policy in force (-1: none chosen)."""
+        v = C.c_int32()
+        _check(lib().ngia_batch_policy(self._h, C.byref(v)))
+        return v.value
 
     def close(self) -> None:
         if self._h:

@@ -52,15 +52,23 @@ def test_batch_sampled_iterations_agree(cuda_device):
 
 
 def test_batch_autotune_keeps_results(cuda_device):
-    """Every job tuned (per length bucket: warp-per-pair cut-off, CTA count,
-    filter tile; jobs of one shape share the cached settings), then the
-    one-loop-per-job form with the tuned settings: still the oracle's
-    clustering per job."""
+    """The batch policy tuner (thread per pair, each job's default cut-off,
+    each job's own per-bucket tuning), then the one-loop-per-job form under
+    every policy: still the oracle's clustering per job."""
     dbs, params = _jobs()
+    want = [oracle.cluster(db.words, db.rec_off, db.type, p.similarity, p.word_length, p.precise)[:2]
+            for db, p in zip(dbs, params)]
     with ngia.Batch(dbs) as b:
+        assert b.policy() == -1
+        with pytest.raises(ngia.NgiaError):
+            b.set_policy(ngia.POLICY_TUNED)  # needs the jobs' own tuning first
         tun = b.autotune(params, 2)
-        assert len(tun) == len(dbs) and all(t["refill"] >= 1 for t in tun)
-        cls, ids, st = b.run(params, ngia.MODE_GRAPH)
-    for db, p, cl, ident in zip(dbs, params, cls, ids):
-        ocl, oid, _ = oracle.cluster(db.words, db.rec_off, db.type, p.similarity, p.word_length, p.precise)
-        assert np.array_equal(cl, ocl) and np.array_equal(ident, oid)
+        assert len(tun) == len(dbs) and all(t["refill"] >= 1 and t["candidates"] == 3 for t in tun)
+        chosen = b.policy()
+        assert chosen in (ngia.POLICY_THREAD, ngia.POLICY_CUTOFF, ngia.POLICY_TUNED)
+        for pol in (chosen, ngia.POLICY_THREAD, ngia.POLICY_CUTOFF, ngia.POLICY_TUNED):
+            b.set_policy(pol)
+            assert b.policy() == pol
+            cls, ids, st = b.run(params, ngia.MODE_GRAPH)
+            for (ocl, oid), cl, ident in zip(want, cls, ids):
+                assert np.array_equal(cl, ocl) and np.array_equal(ident, oid)
