@@ -112,6 +112,25 @@
 #ifndef NGIA_EQ_ZCARRY
 #define NGIA_EQ_ZCARRY 0
 #endif
+//  NGIA_TILE_STRAIGHT  1: a main tile whose rows lie inside the lane's
+//    window and do not wrap around the shared-memory ring loads and stores
+//    them at one base address with immediate offsets, without the per-row
+//    window test, and counts their zeros from one sum of population counts;
+//    NGIA_TILE_STRAIGHT_REM the same for the remainder tiles.  1M DNA
+//    s=0.85: 7.07 -> 6.84 ms per launch (main tiles), 6.82 (both): 0.723 ->
+//    0.749 of the 3-instruction bound.
+//  NGIA_SERVE_STRAIGHT  the same for the tiles with the match table in
+//    global memory (representative per pair).  Off: no difference on the
+//    service (64.1k against 64.7k queries/s capacity, configuration 5).
+#ifndef NGIA_TILE_STRAIGHT
+#define NGIA_TILE_STRAIGHT 1
+#endif
+#ifndef NGIA_TILE_STRAIGHT_REM
+#define NGIA_TILE_STRAIGHT_REM 1
+#endif
+#ifndef NGIA_SERVE_STRAIGHT
+#define NGIA_SERVE_STRAIGHT 0
+#endif
 
 namespace ngia {
 
@@ -124,10 +143,14 @@ constexpr int kAlignThreads = 128;  // threads per CTA of every alignment kernel
 // of the grid (a warp's accesses to one row are one 128-byte line).
 template <int RING>
 struct SmemRing {
+  static constexpr int kSize = RING;
   uint32_t *base;  // ring + threadIdx.x
   __device__ __forceinline__ uint32_t &operator[](int j) const { return base[(j & (RING - 1)) * kAlignThreads]; }
+  __device__ __forceinline__ uint32_t *at(int j) const { return base + (j & (RING - 1)) * kAlignThreads; }
 };
 struct GlobalRing {
+  static constexpr int kSize = 0;  // no straight-tile path
+  __device__ __forceinline__ uint32_t *at(int) const { return nullptr; }
   uint32_t *base;  // scratch + global lane index
   uint32_t mask;   // ring size - 1 (a power of two >= the widest window)
   int64_t stride;  // lanes of the grid
@@ -406,19 +429,57 @@ __device__ __forceinline__ void eq_columns_f(uint32_t (&row)[TW], uint32_t eb, c
 // tiled_tile_eq with the FMA-pipe bookkeeping; s_eq_s is the table's
 // shared-memory address.  NGIA_EQ_NOZOLD: returns the zero count of the
 // tile's rows after the block instead of its change.
-template <int TW, bool PF, class Ring, bool ZC = true>
+// Straight tile: rows base .. base+TW-1 all inside the lane's window
+// (<= je) and contiguous in the shared-memory ring (no wrap).  Its rows are
+// then at rp + m * threads, immediate offsets from one address.
+template <int TW, class Ring>
+__device__ __forceinline__ bool tile_straight(const Ring &ring, int base, int je, uint32_t *&rp) {
+  if constexpr (Ring::kSize >= TW) {
+    rp = ring.at(base);
+    return base + TW - 1 <= je && (base & (Ring::kSize - 1)) + TW <= Ring::kSize;
+  } else {
+    rp = nullptr;
+    return false;
+  }
+}
+template <int TW>
+__device__ __forceinline__ void tile_load_straight(uint32_t (&row)[TW], const uint32_t *rp) {
+#pragma unroll
+  for (int m = 0; m < TW; m++) row[m] = rp[m * kAlignThreads];
+}
+// Stores a straight tile's rows; returns their zero count (ZC) or 0.
+template <int TW, bool ZC>
+__device__ __forceinline__ int tile_store_straight(const uint32_t (&row)[TW], uint32_t *rp) {
+  int ones = 0;
+#pragma unroll
+  for (int m = 0; m < TW; m++) {
+    rp[m * kAlignThreads] = row[m];
+    if (ZC) ones += __popc(row[m]);
+  }
+  return ZC ? 32 * TW - ones : 0;
+}
+
+template <int TW, bool PF, class Ring, bool ZC = true, bool ST = NGIA_TILE_STRAIGHT>
 __device__ __forceinline__ int tiled_tile_eqf(const Ring &ring, uint32_t s_eq_s, int base, int je, int nb1, int cols,
                                               const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw, const FmaK &k) {
   uint32_t row[TW];
   int zold = 0;
+  uint32_t *rp = nullptr;
+  bool straight = false;
+  if constexpr (ST && NGIA_EQ_NOZOLD) straight = tile_straight<TW>(ring, base, je, rp);
+  if (straight) {
+    tile_load_straight<TW>(row, rp);
+  } else {
 #pragma unroll
-  for (int m = 0; m < TW; m++) {
-    const int j = base + m;
-    const bool in = j <= je;
-    row[m] = in ? ring[j] : 0u;
-    if (ZC && !NGIA_EQ_NOZOLD) zold += in ? __popc(~row[m]) : 0;
+    for (int m = 0; m < TW; m++) {
+      const int j = base + m;
+      const bool in = j <= je;
+      row[m] = in ? ring[j] : 0u;
+      if (ZC && !NGIA_EQ_NOZOLD) zold += in ? __popc(~row[m]) : 0;
+    }
   }
   eq_columns_f<TW, true, PF>(row, s_eq_s + 16u * (uint32_t)min(base, nb1), wc, cols, cw, ncw, k);
+  if (straight) return tile_store_straight<TW, ZC>(row, rp);
   int znew = 0;
 #pragma unroll
   for (int m = 0; m < TW; m++) {
@@ -438,7 +499,7 @@ __device__ __forceinline__ int tiled_rem_eqf(int rem, const Ring &ring, uint32_t
   switch (rem) {
 #define NGIA_REM(W) \
   case W:           \
-    if (W < MT) return tiled_tile_eqf<(W < MT ? W : 1), false, Ring, ZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, k); \
+    if (W < MT) return tiled_tile_eqf<(W < MT ? W : 1), false, Ring, ZC, NGIA_TILE_STRAIGHT_REM>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, k); \
     return 0;
     NGIA_REM(1) NGIA_REM(2) NGIA_REM(3) NGIA_REM(4) NGIA_REM(5) NGIA_REM(6) NGIA_REM(7) NGIA_REM(8)
     NGIA_REM(9) NGIA_REM(10) NGIA_REM(11) NGIA_REM(12) NGIA_REM(13) NGIA_REM(14) NGIA_REM(15) NGIA_REM(16)
@@ -510,12 +571,20 @@ template <int TW, bool PF, class Ring>
 __device__ __forceinline__ int tiled_tile_eqfg(const Ring &ring, uint64_t eqb, int base, int je, int nb1, int cols,
                                                const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw, const FmaK &k) {
   uint32_t row[TW];
+  uint32_t *rp = nullptr;
+  bool straight = false;
+  if constexpr (NGIA_SERVE_STRAIGHT != 0) straight = tile_straight<TW>(ring, base, je, rp);
+  if (straight) {
+    tile_load_straight<TW>(row, rp);
+  } else {
 #pragma unroll
-  for (int m = 0; m < TW; m++) {
-    const int j = base + m;
-    row[m] = j <= je ? ring[j] : 0u;
+    for (int m = 0; m < TW; m++) {
+      const int j = base + m;
+      row[m] = j <= je ? ring[j] : 0u;
+    }
   }
   eq_columns_fg<TW, true, PF>(row, eqb + 16ull * (uint64_t)min(base, nb1), wc, cols, cw, ncw, k);
+  if (straight) return tile_store_straight<TW, true>(row, rp);
   int znew = 0;
 #pragma unroll
   for (int m = 0; m < TW; m++) {
