@@ -168,8 +168,9 @@ __global__ void __launch_bounds__(256) k_serve_filter(DevDB qdb, RepStore rs, Ru
 // the tiles with the FMA-pipe bookkeeping of the clustering kernel
 // (tile.cuh); the claimed pairs start in groups that share a representative.
 // 0 (default): every lane reads its pair's table from global memory (L1).
-// Measured on GB300: serving 56.5k vs 59.2k queries/s (configuration 5,
-// 16 slots), speculative rounds of the 20,000-sequence job 0.685 vs 0.507 s.
+// Measured on GB300: serving 56.5k vs 59.2k queries/s (200 batches of
+// 1-4,096 DNA queries against 14,077 representatives, 16 slots), speculative
+// rounds of the 20,000-sequence job 0.685 vs 0.507 s.
 // The kernel is bound by the ALU pipe (80% busy, loads 50%), so the shared
 // tables save little, while groups leave lanes idle (27.7 of 32 active): a
 // claim holds pairs of several representatives, above all in the
@@ -180,8 +181,8 @@ __global__ void __launch_bounds__(256) k_serve_filter(DevDB qdb, RepStore rs, Ru
 // NGIA_SERVE_FMA (DNA, without staging): the per-column bookkeeping on the FMA
 // pipe with the table in global memory (as k_align_tiled does with its
 // shared-memory table).  Measured on GB300: serving 64.3k against 58.9k
-// queries/s (configuration 5, p99 642 against 782 ms), the speculative rounds
-// of the 20,000-sequence job 0.489 against 0.506 s.
+// queries/s (serving 200 DNA query batches, p99 642 against 782 ms), the
+// speculative rounds of the 20,000-sequence job 0.489 against 0.506 s.
 // NGIA_SERVE_REM_ROUND: remainder tiles rounded up to a multiple of this width
 // (fewer tile bodies); 2, 4 and 8 gave 63.5k, 62.2k and 59.1k queries/s.
 #ifndef NGIA_SERVE_FMA

@@ -208,9 +208,10 @@ int run_batch(ngia_server *sv, Slot &sl, Request &rq) {
   // largest round (NGIA_SERVE_MAX_CHUNK, at most kMaxChunk, which sizes the
   // slot's pair queues): a query accepted by a representative of a round can
   // still have its pairs with the round's later representatives aligned.
-  // Swept on GB300 (configuration 5): 1,024, 512, 256 and 128 aligned 300.2M,
-  // 299.3M, 298.5M and 298.0M pairs at 53.1k, 53.0k, 52.3k and 51.3k
-  // queries/s: nearly every pair is one the first-match rule needs.
+  // Swept on GB300 (200 DNA query batches, 14,077 representatives): 1,024,
+  // 512, 256 and 128 aligned 300.2M, 299.3M, 298.5M and 298.0M pairs at
+  // 53.1k, 53.0k, 52.3k and 51.3k queries/s: nearly every pair is one the
+  // first-match rule needs.
   static const int max_chunk = [] {
     const char *m = getenv("NGIA_SERVE_MAX_CHUNK");
     return m ? std::max(kFirstChunk, std::min(kMaxChunk, atoi(m))) : kMaxChunk;
@@ -464,8 +465,9 @@ extern "C" int ngia_serve_open(const ngia_db_view *reps, const ngia_params *para
   sv->prm.word_order = 0;
   if (const char *wo = getenv("NGIA_SERVE_WORD_ORDER")) sv->prm.word_order = std::max(0, std::min(2, atoi(wo)));
   // lockstep refill (NGIA_SERVE_REFILL: idle lanes a warp waits for before it
-  // claims); swept on GB300 (configuration 5): 32, 24, 16, 8 lanes gave
-  // 53.4k, 52.2k, 48.8k, 49.9k queries/s
+  // claims); swept on GB300 (200 DNA query batches, 14,077
+  // representatives): 32, 24, 16, 8 lanes gave 53.4k, 52.2k, 48.8k, 49.9k
+  // queries/s
   sv->prm.refill = 32;
   if (const char *rf = getenv("NGIA_SERVE_REFILL")) sv->prm.refill = std::max(1, std::min(32, atoi(rf)));
   sv->word_first = ngia::word_first_of(sv->type, sv->prm);
