@@ -440,6 +440,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
 
   int state = -1, entry = 0, cand = 0;
   int i = 0, nq = 0, B = 0, js = 0, je = -1, net2 = 0, L2 = 0, cutoff = 0, lastcols = 32, frozen = 0, zw = 0;
+  int zskip = 0;  // query blocks this lane's pair cannot be rejected at (NGIA_ZC_SKIP)
   bool active = false;
   const uint32_t *qpl = nullptr;
   uint32_t cur[P], nxt[P];
@@ -472,6 +473,7 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       je = min(B, nb1 - 1);
       frozen = 0;
       zw = 0;
+      zskip = score_mode ? INT_MAX : 0;
       if (!score_mode) {
         n_pairs++;
         n_cells += (unsigned long long)band_cells(B, nb1, net2);
@@ -501,6 +503,9 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
     bool exact_cover = false;
     if constexpr (kEq && NGIA_EQ_FMA && NGIA_EQ_ZCARRY) exact_cover = __all_sync(kFullMask, !busy || n - MT * full == rem);
     (void)exact_cover;
+    // the warp counts zeros after this block when one of its lanes may be
+    // rejected there
+    const bool cnt = !(kEq && NGIA_EQ_FMA && NGIA_ZC_SKIP) || __any_sync(kFullMask, busy && zskip <= 0);
     if (!busy) continue;
     const int cols = (i == nq - 1) ? lastcols : 32;
     n_done += (unsigned long long)n * cols;
@@ -519,24 +524,24 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       // a one-slot remainder joins the last main tile (warp-uniform)
       const bool merge1 = NGIA_TILED_MERGE1 && rem == 1 && full > 0;
       for (int t = merge1 ? 1 : 0; t < full; t++, base += MT) {
-        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk, cnt);
         last = ncw;
         cw = ncw << (32 - cols);  // column 0's carry at bit 31
         ncw = 0;
       }
       if (merge1) {
-        zw += tiled_tile_eqf<MT + 1, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+        zw += tiled_tile_eqf<MT + 1, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk, cnt);
         last = ncw;
         rem = 0;
       }
       for (; rem >= MT; rem -= MT, base += MT) {
-        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+        zw += tiled_tile_eqf<MT, NGIA_EQ_PF_MAIN, Ring, kZC>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk, cnt);
         last = ncw;
         cw = ncw << (32 - cols);
         ncw = 0;
       }
       if (rem > 0) {
-        zw += tiled_rem_eqf<Ring, MT, kZC>(rem, ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk);
+        zw += tiled_rem_eqf<Ring, MT, kZC>(rem, ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, fk, cnt);
         last = ncw;
       }
       if constexpr (!kZC) {
@@ -605,10 +610,16 @@ __global__ void __launch_bounds__(kAlignThreads, tiled_min_blocks(P))
       state = -1;
       continue;
     }
-    if (!score_mode && frozen + zw + (net2 - 32 * i) < cutoff) {
-      active = false;
-      state = -1;
-      continue;
+    if (cnt) {
+      const int slack = score_mode ? INT_MAX : frozen + zw + (net2 - 32 * i) - cutoff;
+      if (slack < 0) {
+        active = false;
+        state = -1;
+        continue;
+      }
+      zskip = slack >> 5;  // the next blocks whose test cannot fail
+    } else {
+      zskip--;
     }
 #pragma unroll
     for (int p = 0; p < P; p++) cur[p] = nxt[p];

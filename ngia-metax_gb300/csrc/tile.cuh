@@ -97,7 +97,8 @@
 //    one-slot remainder (the dominant 49-block window of 1M DNA s=0.85 is
 //    16+16+16+1), the last main tile and that slot run as one tile of MT+1
 //    slots, saving a tile's per-column overhead.  Off: 0.99x on GB300
-//    (7.15 vs 7.07 ms per launch, 1M DNA s=0.85).
+//    (7.15 vs 7.07 ms per launch, 1M DNA s=0.85; with straight tiles 6.85
+//    against 6.83 ms).
 //  NGIA_WIN_FMA  1: the register-window kernels take each column's code and
 //    the match words' address as multiply-adds on the FMA pipe, as the tiled
 //    kernel does.  Off: no difference on GB300 (the 32-block class of 1M DNA
@@ -128,6 +129,25 @@
 #endif
 #ifndef NGIA_TILE_STRAIGHT_REM
 #define NGIA_TILE_STRAIGHT_REM 1
+#endif
+//  NGIA_ZC_SKIP  1: a warp counts its rows' zeros after a query block only
+//    when one of its lanes could fail the rejection test there.  Zeros
+//    never decrease and the residues left fall by at most 32 per block, so
+//    after a count with slack S = zeros + residues left - cutoff >= 0 the
+//    next floor(S / 32) blocks cannot reject; the pair is rejected at the
+//    same block as with a count after every block.  Off: slower on GB300
+//    (1M DNA s=0.85: 6.88 against 6.83 ms per launch; the warp vote and the
+//    branch cost more than the population counts they skip).
+#ifndef NGIA_ZC_SKIP
+#define NGIA_ZC_SKIP 0
+#endif
+//  NGIA_EQ_PF_REM  1: the remainder tiles also load the next column's match
+//    words during the current one.  Off: the tiled launch alone 6.75 against
+//    6.83 ms (plain-driver replay), but the graph-driven iterations, where
+//    the length buckets' launches overlap, no faster (136.15M against
+//    136.17M candidate seqs/s).
+#ifndef NGIA_EQ_PF_REM
+#define NGIA_EQ_PF_REM 0
 #endif
 #ifndef NGIA_SERVE_STRAIGHT
 #define NGIA_SERVE_STRAIGHT 0
@@ -450,19 +470,20 @@ __device__ __forceinline__ void tile_load_straight(uint32_t (&row)[TW], const ui
 }
 // Stores a straight tile's rows; returns their zero count (ZC) or 0.
 template <int TW, bool ZC>
-__device__ __forceinline__ int tile_store_straight(const uint32_t (&row)[TW], uint32_t *rp) {
+__device__ __forceinline__ int tile_store_straight(const uint32_t (&row)[TW], uint32_t *rp, bool cnt = true) {
+#pragma unroll
+  for (int m = 0; m < TW; m++) rp[m * kAlignThreads] = row[m];
+  if (!ZC || !cnt) return 0;
   int ones = 0;
 #pragma unroll
-  for (int m = 0; m < TW; m++) {
-    rp[m * kAlignThreads] = row[m];
-    if (ZC) ones += __popc(row[m]);
-  }
-  return ZC ? 32 * TW - ones : 0;
+  for (int m = 0; m < TW; m++) ones += __popc(row[m]);
+  return 32 * TW - ones;
 }
 
 template <int TW, bool PF, class Ring, bool ZC = true, bool ST = NGIA_TILE_STRAIGHT>
 __device__ __forceinline__ int tiled_tile_eqf(const Ring &ring, uint32_t s_eq_s, int base, int je, int nb1, int cols,
-                                              const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw, const FmaK &k) {
+                                              const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw, const FmaK &k,
+                                              bool cnt = true) {
   uint32_t row[TW];
   int zold = 0;
   uint32_t *rp = nullptr;
@@ -480,14 +501,14 @@ __device__ __forceinline__ int tiled_tile_eqf(const Ring &ring, uint32_t s_eq_s,
     }
   }
   eq_columns_f<TW, true, PF>(row, s_eq_s + 16u * (uint32_t)min(base, nb1), wc, cols, cw, ncw, k);
-  if (straight) return tile_store_straight<TW, ZC>(row, rp);
+  if (straight) return tile_store_straight<TW, ZC>(row, rp, cnt);
   int znew = 0;
 #pragma unroll
   for (int m = 0; m < TW; m++) {
     const int j = base + m;
     if (j <= je) {
       ring[j] = row[m];
-      if (ZC) znew += __popc(~row[m]);
+      if (ZC && cnt) znew += __popc(~row[m]);
     }
   }
   return znew - zold;
@@ -496,11 +517,11 @@ __device__ __forceinline__ int tiled_tile_eqf(const Ring &ring, uint32_t s_eq_s,
 template <class Ring, int MT, bool ZC = true>
 __device__ __forceinline__ int tiled_rem_eqf(int rem, const Ring &ring, uint32_t s_eq_s, int base, int je, int nb1,
                                              int cols, const uint32_t (&wc)[2], uint32_t &cw, uint32_t &ncw,
-                                             const FmaK &k) {
+                                             const FmaK &k, bool cnt = true) {
   switch (rem) {
 #define NGIA_REM(W) \
   case W:           \
-    if (W < MT) return tiled_tile_eqf<(W < MT ? W : 1), false, Ring, ZC, NGIA_TILE_STRAIGHT_REM>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, k); \
+    if (W < MT) return tiled_tile_eqf<(W < MT ? W : 1), NGIA_EQ_PF_REM != 0, Ring, ZC, NGIA_TILE_STRAIGHT_REM>(ring, s_eq_s, base, je, nb1, cols, wc, cw, ncw, k, cnt); \
     return 0;
     NGIA_REM(1) NGIA_REM(2) NGIA_REM(3) NGIA_REM(4) NGIA_REM(5) NGIA_REM(6) NGIA_REM(7) NGIA_REM(8)
     NGIA_REM(9) NGIA_REM(10) NGIA_REM(11) NGIA_REM(12) NGIA_REM(13) NGIA_REM(14) NGIA_REM(15) NGIA_REM(16)
