@@ -124,6 +124,15 @@ __global__ void __launch_bounds__(512) k_pool_prep(PoolDev pd) {
 // Per bucket: the chunk size of this round (about eight chunks per CTA of the
 // bucket's launch, 128 to 4,096 pairs) and the exclusive prefix of every
 // job's chunk count.  Run by the last CTA of the filter (NT threads).
+// Chunk size of a bucket: its pairs over NGIA_POOL_CHUNK_DIV chunks per CTA
+// of the alignment grid, at least NGIA_POOL_CHUNK_MIN and at most 4,096
+// pairs.  A CTA's warps meet at a barrier between chunks.
+#ifndef NGIA_POOL_CHUNK_DIV
+#define NGIA_POOL_CHUNK_DIV 8
+#endif
+#ifndef NGIA_POOL_CHUNK_MIN
+#define NGIA_POOL_CHUNK_MIN 128
+#endif
 template <int NT>
 __device__ void chunks_body(const PoolDev &pd, int ncls) {
   __shared__ long long s_red[NT / 32];
@@ -142,8 +151,9 @@ __device__ void chunks_body(const PoolDev &pd, int ncls) {
     if (t == 0) {
       long long T = 0;
       for (int i = 0; i < NT / 32; i++) T += s_red[i];
-      const long long want = (T + 8ll * pd.grid_align[k] - 1) / (8ll * pd.grid_align[k]);
-      s_C = (int)max(128ll, min(4096ll, want));
+      const long long per = (long long)NGIA_POOL_CHUNK_DIV * pd.grid_align[k];
+      const long long want = (T + per - 1) / per;
+      s_C = (int)max((long long)NGIA_POOL_CHUNK_MIN, min(4096ll, want));
     }
     __syncthreads();
     const int C = s_C;
