@@ -126,7 +126,9 @@ __global__ void __launch_bounds__(512) k_pool_prep(PoolDev pd) {
 // job's chunk count.  Run by the last CTA of the filter (NT threads).
 // Chunk size of a bucket: its pairs over NGIA_POOL_CHUNK_DIV chunks per CTA
 // of the alignment grid, at least NGIA_POOL_CHUNK_MIN and at most 4,096
-// pairs.  A CTA's warps meet at a barrier between chunks.
+// pairs.  A CTA's warps meet at a barrier between chunks.  Swept on GB300
+// (256-job batch, 8 iterations per job): 16/64, 8/128, 4/256 and 2/512 gave
+// 13.7M, 17.0M, 16.2M and 15.3M candidate seqs/s.
 #ifndef NGIA_POOL_CHUNK_DIV
 #define NGIA_POOL_CHUNK_DIV 8
 #endif
