@@ -37,10 +37,22 @@ __host__ __device__ inline int generic_class(int type) { return num_classes(type
 __host__ __device__ inline bool is_tiled_class(int type, int c) {
   return c == generic_class(type) - 1 || c == generic_class(type) - 2;
 }
+// DNA register-window classes in use (caps 8, 16, 24, 32 blocks, in that
+// order); windows above the last one in use go to the 64-block tiled class.
+// Two: windows of 17-64 blocks share the tiled class's persistent launch,
+// where their pairs fill the launch's tail instead of running as separate
+// latency-bound launches beside it.  Measured on GB300 (1M DNA s=0.85,
+// graph driver): 4, 3, 2 and 0 classes gave 136.1M, 137.6M, 138.0M and
+// 138.0M candidate seqs/s.
+#ifndef NGIA_DNA_WIN_CLASSES
+#define NGIA_DNA_WIN_CLASSES 2
+#endif
 __host__ __device__ inline int class_of(int type, int A) {
   const int g = generic_class(type);
-  for (int c = 0; c < g; c++)
+  for (int c = 0; c < g; c++) {
+    if (type == 0 && c < 4 && c >= NGIA_DNA_WIN_CLASSES) continue;
     if (A <= class_cap(type, c)) return c;
+  }
   return g;
 }
 
