@@ -227,7 +227,8 @@ int alloc_db(ngia_ctx *c, int type, int64_t cap_n, int64_t cap_words) {
   const int A = ngia::count_words(type);
   if (dalloc(&c->d_words, (size_t)cap_words + 4) != cudaSuccess || dalloc(&c->d_off, (size_t)cap_n) != cudaSuccess ||
       dalloc(&c->d_len, (size_t)cap_n) != cudaSuccess || dalloc(&c->d_net, (size_t)cap_n) != cudaSuccess ||
-      dalloc(&c->d_cnt, (size_t)cap_n * A) != cudaSuccess)
+      dalloc(&c->d_cnt, (size_t)cap_n * A) != cudaSuccess ||
+      (type != 0 && dalloc(&c->d_codes, (size_t)cap_words + 4) != cudaSuccess))
     return fail(NGIA_E_NOMEM, "ngia_open: device allocation of the database failed");
   c->cap_n = cap_n;
   c->cap_words = cap_words;
@@ -236,6 +237,7 @@ int alloc_db(ngia_ctx *c, int type, int64_t cap_n, int64_t cap_words) {
   c->db.len = c->d_len;
   c->db.net = c->d_net;
   c->db.cnt = c->d_cnt;
+  c->db.codes = c->d_codes;
   c->db.n = 0;
   c->db.type = type;
   c->db.hw = ngia::header_words(type);
@@ -436,6 +438,7 @@ extern "C" int ngia_close(ngia_ctx *c) {
   cudaFree(c->d_len);
   cudaFree(c->d_net);
   cudaFree(c->d_cnt);
+  cudaFree(c->d_codes);
   ngia::RunBufs &rb = c->rb;
   cudaFree(rb.st);
   cudaFree(rb.cluster);

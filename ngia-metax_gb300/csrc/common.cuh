@@ -63,6 +63,9 @@ struct DevDB {
   const int32_t *len;     // raw length (record word 0)
   const int32_t *net;     // net length (record word 1)
   const uint32_t *cnt;    // residue counts, 4 (DNA) or 28 (protein) per sequence
+  const uint32_t *codes;  // protein: each record's residue codes as a bit stream
+                          // (5 words per 32-residue block, at the planes'
+                          // offsets); null for DNA
   int32_t n, type;
   int32_t hw, P, A;       // header words, planes, count words
   int32_t max_nb;         // max plane blocks over all records

@@ -21,6 +21,7 @@ struct ngia_ctx {
   int64_t *d_off = nullptr;
   int32_t *d_len = nullptr, *d_net = nullptr;
   uint32_t *d_cnt = nullptr;
+  uint32_t *d_codes = nullptr;  // protein residue-code streams (DevDB::codes)
   int64_t n_words = 0;
   int32_t longest = 0;
   // capacity of the allocations (a context can be reloaded with any database

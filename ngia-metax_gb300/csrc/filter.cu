@@ -54,10 +54,48 @@ __global__ void k_loader(const uint32_t *__restrict__ words, const int64_t *__re
   if (local_bad) atomicOr(bad, 1);
 }
 
+// Protein residue-code streams, one warp per record (lanes over its
+// blocks): each 32-residue block's five plane words become five stream
+// words holding the block's residue codes (plane p = bit p of a code) as
+// 5-bit groups, residue 0 at the top: residue j's code fills bits 155-5j ..
+// 159-5j of the block's 160-bit value, whose bits 159..128 are stream word 0.
+// Read across blocks, the stream holds every w-mer of the record in 5w
+// contiguous bits with its last residue lowest, as the short-word test's
+// rolling word holds it (func.cu:376-396).  Records the loader rejected have
+// length 0 and are skipped.
+__global__ void k_codes(const uint32_t *__restrict__ words, const int64_t *__restrict__ off,
+                        const int32_t *__restrict__ len, int n, int hw, uint32_t *__restrict__ codes) {
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t c = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < n; c += nw) {
+    const int nb = (len[c] + 31) >> 5;
+    const int64_t base = off[c] + hw;
+    for (int b = lane; b < nb; b += 32) {
+      uint32_t pl[5], st[5] = {0u, 0u, 0u, 0u, 0u};
+#pragma unroll
+      for (int p = 0; p < 5; p++) pl[p] = words[base + 5 * b + p];
+#pragma unroll
+      for (int j = 0; j < 32; j++) {
+        uint32_t cj = 0;
+#pragma unroll
+        for (int p = 0; p < 5; p++) cj |= ((pl[p] >> j) & 1u) << p;
+        const int t = 155 - 5 * j;  // the code's lowest bit in the 160-bit value
+        const int k = 4 - (t >> 5), sh = t & 31;
+        st[k] |= cj << sh;
+        if (sh > 27) st[k - 1] |= cj >> (32 - sh);  // the group crosses into the word above
+      }
+#pragma unroll
+      for (int k = 0; k < 5; k++) codes[base + 5 * b + k] = st[k];
+    }
+  }
+}
+
 cudaError_t launch_loader(ngia_ctx *c, int32_t *d_maxnb, int32_t *d_short, int32_t *d_bad) {
   int grid = c->num_sms * 4;
   k_loader<<<grid, 256, 0, c->stream>>>(c->d_words, c->d_off, c->n_words, c->db.n, c->db.type, c->d_len,
                                         c->d_net, c->d_cnt, d_maxnb, d_short, d_bad);
+  if (c->db.type != 0 && c->d_codes)
+    k_codes<<<grid, 256, 0, c->stream>>>(c->d_words, c->d_off, c->d_len, c->db.n, c->db.hw, c->d_codes);
   return cudaGetLastError();
 }
 
@@ -251,6 +289,92 @@ __device__ int word_count_fast(const uint32_t *__restrict__ planes, int net2, in
   }
 }
 
+// ---- protein short-word count on the residue-code stream (k_codes) -----------
+// The w-mer ending at residue j of a block: the 5w bits ending 5(j+1) bits
+// below the top of the block's stream words st[], the previous block's last
+// word above them (prev; 0 before the first block).  One funnel shift.
+__device__ __forceinline__ uint32_t codes_word(const uint32_t (&st)[5], uint32_t prev, int j) {
+  const int e = 5 * (j + 1), k = (e - 1) >> 5;
+  return __funnelshift_r(st[k], k ? st[k - 1] : prev, 32 * (k + 1) - e);
+}
+
+// Lookups of the first lim (<= 32) positions of one block.
+__device__ __forceinline__ int codes_block(const uint32_t *__restrict__ blk, uint32_t prev, int lim, uint32_t mask,
+                                           const uint8_t *tab, uint32_t &last) {
+  uint32_t st[5];
+#pragma unroll
+  for (int k = 0; k < 5; k++) st[k] = __ldg(blk + k);
+  int sum = 0;
+  if (lim == 32) {
+#pragma unroll
+    for (int j = 0; j < 32; j++) sum += tab[codes_word(st, prev, j) & mask];
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; j++)
+      if (j < lim) sum += tab[codes_word(st, prev, j) & mask];
+  }
+  last = st[4];
+  return sum;
+}
+
+// The first w-1 positions (zero history), counted by the loops and subtracted.
+__device__ __forceinline__ int codes_head(const uint32_t *__restrict__ codes, int net2, int w, uint32_t mask,
+                                          const uint8_t *tab) {
+  const int head = min(w - 1, net2);
+  if (head <= 0) return 0;
+  uint32_t st[5];
+#pragma unroll
+  for (int k = 0; k < 5; k++) st[k] = __ldg(codes + k);
+  int sum = 0;
+#pragma unroll
+  for (int j = 0; j < 7; j++)
+    if (j < head) sum += tab[codes_word(st, 0u, j) & mask];
+  return sum;
+}
+
+// Short-word count of one protein candidate by one thread.
+__device__ int word_count_codes(const uint32_t *__restrict__ codes, int net2, int w, const uint8_t *tab) {
+  const uint32_t mask = (1u << (5 * w)) - 1u;
+  const int nb = (net2 + 31) >> 5;
+  uint32_t prev = 0;
+  int sum = 0;
+  for (int b = 0; b < nb; b++) sum += codes_block(codes + 5 * b, prev, min(32, net2 - 32 * b), mask, tab, prev);
+  return sum - codes_head(codes, net2, w, mask, tab);
+}
+
+// The same by the whole warp: lane l takes blocks l, l+32, ..., the previous
+// block's last stream word from the lane below.  All 32 lanes call it with
+// the same arguments.
+__device__ int word_count_codes_warp(const uint32_t *__restrict__ codes, int net2, int w, const uint8_t *tab) {
+  const uint32_t mask = (1u << (5 * w)) - 1u;
+  const int lane = threadIdx.x & 31;
+  const int nb = (net2 + 31) >> 5;
+  int sum = 0;
+  uint32_t carry = 0;  // last stream word of the block below lane 0's
+  for (int b0 = 0; b0 < nb; b0 += 32) {
+    const int b = b0 + lane;
+    const int lim = b < nb ? min(32, net2 - 32 * b) : 0;
+    const uint32_t last_mine = b < nb ? __ldg(codes + 5 * b + 4) : 0u;
+    uint32_t prev = __shfl_up_sync(kFullMask, last_mine, 1);
+    if (lane == 0) prev = carry;
+    uint32_t last = 0;
+    if (lim > 0) sum += codes_block(codes + 5 * b, prev, lim, mask, tab, last);
+    carry = __shfl_sync(kFullMask, last_mine, 31);
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFullMask, sum, o);
+  return sum - codes_head(codes, net2, w, mask, tab);
+}
+
+// Short-word count of candidate c for the filter: protein from the code
+// stream when the database has one, otherwise from the planes.
+template <int P>
+__device__ __forceinline__ int word_count_cand(const DevDB &db, int c, int net2, int w, const uint8_t *tab) {
+  const int64_t o = __ldg(db.off + c) + db.hw;
+  if (P == 5 && db.codes) return word_count_codes(db.codes + o, net2, w, tab);
+  return word_count_fast<P>(db.words + o, net2, w, tab);
+}
+
 // Short-word count of one candidate by the whole warp: lane l takes blocks
 // l, l+32, ...; each lane's history (the previous block) comes from the lane
 // below by a shuffle.  All 32 lanes call it with the same arguments.
@@ -298,6 +422,13 @@ __device__ int word_count_warp(const uint32_t *__restrict__ planes, int net2, in
   for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(kFullMask, sum, o);
   if (P == 2) return sum - dna_head(planes, net2, w, mask, tab);
   return sum - roll_head<P>(planes, net2, w, mask, tab);
+}
+
+template <int P>
+__device__ __forceinline__ int word_count_cand_warp(const DevDB &db, int c, int net2, int w, const uint8_t *tab) {
+  const int64_t o = __ldg(db.off + c) + db.hw;
+  if (P == 5 && db.codes) return word_count_codes_warp(db.codes + o, net2, w, tab);
+  return word_count_warp<P>(db.words + o, net2, w, tab);
 }
 
 // Candidates longer than this are counted by the whole warp.
@@ -447,8 +578,7 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
           wchk++;
           bytes += 4ull * P * ((net2 + 31) / 32);
           if (net2 <= kWarpWordLen) {
-            const uint32_t *planes = db.words + __ldg(db.off + c) + db.hw;
-            pass = !(word_count_fast<P>(planes, net2, prm.w, s_tab) < word_min(L2, prm.w, s));
+            pass = !(word_count_cand<P>(db, c, net2, prm.w, s_tab) < word_min(L2, prm.w, s));
             if (pass) wpass++;
           } else {
             deferred = true;
@@ -530,8 +660,7 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
           wchk++;
           bytes += 4ull * P * ((net2 + 31) / 32);
           if (net2 <= kWarpWordLen) {
-            const uint32_t *planes = db.words + __ldg(db.off + c) + db.hw;
-            pass = !(word_count_fast<P>(planes, net2, prm.w, s_tab) < word_min(L2, prm.w, s));
+            pass = !(word_count_cand<P>(db, c, net2, prm.w, s_tab) < word_min(L2, prm.w, s));
             if (pass) wpass++;
           } else {
             deferred = true;
@@ -543,8 +672,7 @@ __global__ void __launch_bounds__(256) k_filter(DevDB db, RunBufs rb, RunParams 
       for (unsigned dm = __ballot_sync(kFullMask, deferred); dm; dm &= dm - 1) {
         const int src = __ffs(dm) - 1;
         const int cc = wi * 32 + src;
-        const uint32_t *planes = db.words + __ldg(db.off + cc) + db.hw;
-        const int ws = word_count_warp<P>(planes, __ldg(db.net + cc), prm.w, s_tab);
+        const int ws = word_count_cand_warp<P>(db, cc, __ldg(db.net + cc), prm.w, s_tab);
         if (lane == src) {
           const int L2 = __ldg(db.len + cc);
           pass = !(ws < word_min(L2, prm.w, s));
@@ -725,8 +853,7 @@ __global__ void __launch_bounds__(256) k_filter_long(DevDB db, RunBufs rb, RunPa
   unsigned long long wpass = 0;
   for (int k = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < nlong; k += W) {
     const int c = rb.long_list[k];
-    const uint32_t *planes = db.words + __ldg(db.off + c) + db.hw;
-    const int ws = word_count_warp<P>(planes, __ldg(db.net + c), prm.w, s_tab);
+    const int ws = word_count_cand_warp<P>(db, c, __ldg(db.net + c), prm.w, s_tab);
     const int L2 = __ldg(db.len + c);
     const bool pass = lane == 0 && !(ws < word_min(L2, prm.w, s));
     if (pass) wpass++;
