@@ -225,10 +225,14 @@ int create_streams(ngia_ctx *c) {
 // Device arrays of a database of up to cap_n records and cap_words words.
 int alloc_db(ngia_ctx *c, int type, int64_t cap_n, int64_t cap_words) {
   const int A = ngia::count_words(type);
+  // protein residue-code streams for the short-word test (NGIA_PROTEIN_CODES=0:
+  // the test reads the planes instead)
+  const char *pc = getenv("NGIA_PROTEIN_CODES");
+  const bool codes = type != 0 && !(pc && atoi(pc) == 0);
   if (dalloc(&c->d_words, (size_t)cap_words + 4) != cudaSuccess || dalloc(&c->d_off, (size_t)cap_n) != cudaSuccess ||
       dalloc(&c->d_len, (size_t)cap_n) != cudaSuccess || dalloc(&c->d_net, (size_t)cap_n) != cudaSuccess ||
       dalloc(&c->d_cnt, (size_t)cap_n * A) != cudaSuccess ||
-      (type != 0 && dalloc(&c->d_codes, (size_t)cap_words + 4) != cudaSuccess))
+      (codes && dalloc(&c->d_codes, (size_t)cap_words + 4) != cudaSuccess))
     return fail(NGIA_E_NOMEM, "ngia_open: device allocation of the database failed");
   c->cap_n = cap_n;
   c->cap_words = cap_words;
