@@ -61,7 +61,7 @@ struct ngia_batch {
   // under it, restored on every NGIA_MODE_GRAPH run
   int policy = -1;
   std::vector<int> policy_wp;
-  std::vector<ngia_tuning> own;  // each job's own tuning (ngia_batch_autotune)
+  std::vector<ngia_tuning> own;  // each job's own tuning, once ngia_batch_autotune found it
 };
 
 namespace {
@@ -447,12 +447,12 @@ extern "C" int ngia_batch_autotune(ngia_batch *b, const ngia_params *params, int
   if (!b || !params || iters <= 0) return fail(NGIA_E_ARG, "ngia_batch_autotune: bad argument");
   const size_t nj = b->jobs.size();
   // every job's own tuning, found alone (cached by database shape)
-  b->own.assign(nj, ngia_tuning{});
-  std::vector<ngia_tuning> &own = b->own;
+  std::vector<ngia_tuning> own(nj);
   for (size_t j = 0; j < nj; j++) {
     int rc = ngia_autotune(b->jobs[j], &params[j], iters, &own[j]);
     if (rc) return rc;
   }
+  b->own = own;
   // each policy timed on the whole batch, the first `iters` iterations of
   // every job in one graph launch: one untimed launch (graph capture), then
   // the faster of two
@@ -492,10 +492,11 @@ extern "C" int ngia_batch_set_policy(ngia_batch *b, int32_t policy) {
   ngia::clear_error();
   if (!b || policy < NGIA_BATCH_POLICY_THREAD || policy > NGIA_BATCH_POLICY_TUNED)
     return fail(NGIA_E_ARG, "ngia_batch_set_policy: bad argument");
-  if (policy == NGIA_BATCH_POLICY_TUNED && b->own.size() != b->jobs.size())
+  const bool have_own = b->own.size() == b->jobs.size();
+  if (policy == NGIA_BATCH_POLICY_TUNED && !have_own)
     return fail(NGIA_E_STATE, "ngia_batch_set_policy: the jobs' own settings come from ngia_batch_autotune");
-  if (b->own.size() != b->jobs.size()) b->own.assign(b->jobs.size(), ngia_tuning{});
-  return apply_policy(b, policy, b->own);
+  // the untuned policies do not read the jobs' own settings
+  return apply_policy(b, policy, have_own ? b->own : std::vector<ngia_tuning>(b->jobs.size()));
 }
 
 extern "C" int ngia_batch_policy(const ngia_batch *b, int32_t *policy) {
