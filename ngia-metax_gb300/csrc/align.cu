@@ -834,6 +834,9 @@ static AlignFn warp_fn(int type, int cls) {
   return type == 0 ? k_align_warp<2> : k_align_warp<5>;
 }constexpr int kWarpKernel = kNumClasses;  // index of the warp kernel in the attribute table
 
+// DNA buckets 2 and 3 (windows of 17-32 blocks) receive pairs only when
+// NGIA_DNA_WIN_CLASSES (common.cuh) keeps them; by default those windows go
+// to bucket 4, the 64-slot tiled kernel.
 static AlignFn align_fn(int type, int cls) {
   if (type == 0) {
     switch (cls) {
